@@ -1,0 +1,419 @@
+#!/usr/bin/env python3
+"""Benchmark of the stencil3d hot path on GB300.
+
+Workload (default): the 25-point cross stencil (radius 4, the reference's
+stencil_25.h coefficients) in its leapfrog wave form, 1024^3 interior with
+4-point halos, FP32 fields; Gaussian-blob initial field (8 seeded blobs,
+sigma = 20 cells, v = u), 15 Hz Ricker point source at the grid centre,
+c = 1500 m/s, dx = 10 m, dt = 0.5 ms.  Synthetic data: the reference ships
+no dataset.
+
+One step = one leapfrog time step over the whole grid (one kernel launch).
+``value`` is whole-job throughput in Gpoints/s with the fields resident in
+HBM; ``e2e`` is the same metric through the drop-in C-ABI call
+``st3d_iterate_host`` (ITERATE's replacement) on pinned host arrays, host
+to device and device to host copies inside the timed region.  Fields are
+13.4 GB, far larger than the 129 MB L2, so no flush is needed between steps.
+
+``--impl reference`` times the CPU restatement of the path (the oracle; the
+reference's own compiled path where it runs on this machine) with every host
+core on the same workload, one full time step per step.
+
+Multi-GPU: the path does not shard (a single grid would need a halo
+exchange the reference does not have), so ``--gpus N`` under torchrun runs N
+independent replicas, one grid per GPU (weak scaling), barrier and max-over-
+ranks timing over gloo.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    # name: (points, xs, ys, zs, halo, dt, init)
+    "wave25_1024": (25, 1024, 1024, 1024, 4, 5e-4, "blobs"),
+    "wave25_528": (25, 528, 528, 528, 4, 5e-4, "uniform"),
+    "wave13_1040": (13, 1040, 1040, 1040, 2, 5e-4, "blobs"),
+    "wave7_256": (7, 256, 256, 256, 1, 1e-3, "uniform"),
+}
+SEED = 20251203
+
+
+def parse():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="wave25_1024")
+    p.add_argument("--kernel", choices=["auto", "simple", "tma"], default="auto")
+    p.add_argument("--accuracy-steps", type=int, default=1000,
+                   help="steps of the FP32-vs-FP64 drift run (0: skip)")
+    p.add_argument("--e2e-calls", type=int, default=3)
+    p.add_argument("--e2e-iters", type=int, default=20,
+                   help="time steps per drop-in call (the README host run uses --iter 20)")
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="target CPU time of the cpu_baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# --------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# --------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.2)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_tag, workload):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (profiles/<kernel>_<workload>.md, line 'traffic_bytes_per_launch:')."""
+    path = os.path.join(REPO, "profiles", "%s_%s.md" % (kernel_tag, workload))
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+# --------------------------------------------------------------------------
+def make_stencil(S, wl, storage="f32", kernel="auto"):
+    points, xs, ys, zs, halo, dt, init = WORKLOADS[wl]
+    g = S.Grid(xs, ys, zs, halo, halo, halo)
+    st = S.Stencil(g, points, "wave", storage, kernel=kernel, dt=dt,
+                   src=(xs // 2, ys // 2, zs // 2))
+    init_fields(S, st, init)
+    return g, st
+
+
+def init_fields(S, st, init):
+    if init == "blobs":
+        st.fill(S.FIELD_U, S.FILL_BLOBS, SEED, 8, 20.0)
+        st.fill(S.FIELD_V, S.FILL_BLOBS, SEED, 8, 20.0)
+    else:
+        st.fill(S.FIELD_U, S.FILL_UNIFORM, SEED, -1e-3, 1e-3)
+        st.fill(S.FIELD_V, S.FILL_UNIFORM, SEED + 1, -1e-3, 1e-3)
+    st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
+    st.synchronize()
+
+
+def accuracy_run(S, wl, steps, kernel):
+    """FP32 and FP64 runs of the same workload; relative L2 and max error of
+    u against FP64 every 100 steps (FP64 reductions on the device)."""
+    g, a = make_stencil(S, wl, "f32", kernel)
+    _, b = make_stencil(S, wl, "f64")
+    report = []
+    done = 0
+    while done < steps:
+        n = min(100, steps - done)
+        a.iterate(n)
+        b.iterate(n)
+        a.synchronize()
+        b.synchronize()
+        done += n
+        d2, b2, dm, bm = a.norms(S.FIELD_U, b, S.FIELD_U)
+        report.append({"step": done, "rel_l2": (d2 / b2) ** 0.5 if b2 > 0 else None,
+                       "max_abs": dm, "rel_max": dm / bm if bm > 0 else None})
+    a.close()
+    b.close()
+    return report
+
+
+def e2e_run(S, st, g, calls, iters):
+    """Drop-in calls on pinned host arrays: upload v, s, u; `iters` steps;
+    download v and u; CUDA events on the context's stream bracket it all."""
+    shape = g.shape
+    pv, ps, pu = S.PinnedArray(shape), S.PinnedArray(shape), S.PinnedArray(shape)
+    try:
+        st.download(pv.array, pu.array)  # current device state as the host input
+        ps.array[...] = 0.0
+        st.iterate_host(pv.array, ps.array, pu.array, iters)  # warm-up call
+        times = []
+        for _ in range(calls):
+            st.timer_start()
+            st.iterate_host(pv.array, ps.array, pu.array, iters)
+            times.append(st.timer_stop())
+        host = (pv.array.copy(), pu.array.copy())
+    finally:
+        for p in (pv, ps, pu):
+            p.free()
+    pts = g.gvol
+    ms = statistics.median(times)
+    # bytes copied per call, counted from the copied regions
+    xs, ys, zs = g.xsize, g.ysize, g.zsize
+    h = min(g.xhalo, 4)
+    h2d = 3 * (xs + 2 * h) * (ys + 2 * h) * (zs + 2 * h) * 4
+    d2h = 2 * xs * ys * zs * 4
+    return {"value": pts * iters / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "step": "one ITERATE-equivalent call (st3d_iterate_host) of %d time steps" % iters,
+            "ms_per_call": ms}, host
+
+
+def cpu_wave_sample(wl, u, v, target_s, threads):
+    """Time the CPU restatement (oracle, plain flavour, OpenMP) of the same
+    leapfrog update on the same fields: one full time step per sample step."""
+    from oracle import oracle as O
+    points, xs, ys, zs, halo, dt, init = WORKLOADS[wl]
+    grid = (xs, ys, zs, halo, halo, halo)
+    c0, c1, c2 = O.wave_constants(points, 1500.0, dt, 10.0)
+    s = np.zeros_like(u)
+    src = (xs // 2, ys // 2, zs // 2)
+    amps = O.ricker_amps(0, 10000, dt)
+    t0 = time.perf_counter()
+    O.iterate_wave(u, v, s, grid, points, 1, c0, c1, c2, src=src, amps=amps, fma=False)
+    one = time.perf_counter() - t0
+    n = max(2, min(200, int(target_s / max(one, 1e-6))))
+    n += n % 2  # even: no trailing copy of the newest field back into u
+    t0 = time.perf_counter()
+    O.iterate_wave(u, v, s, grid, points, n, c0, c1, c2, src=src, amps=amps[1:], fma=False)
+    el = time.perf_counter() - t0
+    return {"value": xs * ys * zs * n / el / 1e9, "unit": "Gpts/s", "cores": threads,
+            "kind": "port",
+            "sample": "%d full %s leapfrog steps (%.1f s) of the oracle's C restatement, "
+                      "OpenMP %d threads" % (n, wl, el, threads)}
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# --------------------------------------------------------------------------
+def run_gb300(args, dist):
+    import stencil3d_gb300 as S
+    points, xs, ys, zs, halo, dt, init = WORKLOADS[args.workload]
+    g, st = make_stencil(S, args.workload, "f32", args.kernel)
+    info = st.info()
+    st.iterate(args.warmup)
+    st.synchronize()
+
+    dist.barrier()
+    st.synchronize()
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    launches0 = st.info().launches
+    st.timer_start()
+    st.iterate(args.steps)
+    ms = st.timer_stop()
+    st.synchronize()
+    launches = st.info().launches - launches0
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+
+    pts = g.gvol
+    value = dist.world * pts * args.steps / (ms_max * 1e-3) / 1e9
+    launch_ms = ms / max(1, launches)
+    peak, peak_kind = measured_peak()
+    achieved = info.bytes_per_point * pts / (launch_ms * 1e-3) / 1e9
+    kernel_tag = "tma" if info.kernel == S.KERNEL_TMA else "simple"
+    traffic = profile_traffic(kernel_tag, args.workload)
+
+    result = {
+        "metric": "Gpts/s + % of HBM roofline, 25-pt 1024^3: FP32 vs FP16-store at stated L2 err",
+        "value": value, "unit": "Gpts/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded Gaussian blobs + Ricker source (no dataset in the reference)",
+        "config": {"workload": args.workload, "points": points, "grid": [xs, ys, zs],
+                   "halo": halo, "form": "leapfrog wave", "dt": dt, "storage": "f32",
+                   "kernel": kernel_tag, "tile_j": info.tile_j, "tile_k": info.tile_k,
+                   "ichunk": info.ichunk,
+                   "l2": "fields 13.4 GB >> 129 MB L2, no flush needed",
+                   "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+        "gflops": pts * args.steps * info.flops_per_point / (ms * 1e-3) / 1e9,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "bytes_per_point": info.bytes_per_point,
+                     "traffic": traffic,
+                     "kernel": "k_tma<%d,wave>" % points if kernel_tag == "tma" else
+                               "k_simple<float,%d,wave>" % points},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "fp16": None,
+    }
+
+    if dist.rank == 0 and args.accuracy_steps > 0:
+        result["accuracy_vs_fp64"] = accuracy_run(S, args.workload, args.accuracy_steps,
+                                                  args.kernel)
+        result["l2_err_fp32_vs_fp64"] = result["accuracy_vs_fp64"][-1]["rel_l2"]
+
+    host = None
+    if args.e2e_calls > 0:
+        e2e, host = e2e_run(S, st, g, args.e2e_calls, args.e2e_iters)
+        e2e["value"] = dist.world * e2e["value"] if dist.world > 1 else e2e["value"]
+        result["e2e"] = e2e
+    st.close()
+
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and host is not None:
+        v_host, u_host = host
+        result["cpu_baseline"] = cpu_wave_sample(args.workload, u_host, v_host,
+                                                 args.cpu_seconds, host_threads())
+    if dist.rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def run_reference(args, dist):
+    """The reference arm: the CPU implementation of the path on the host
+    cores, same workload and metric.  Rank 0 alone runs it."""
+    if dist.rank != 0:
+        return
+    from oracle import build as obuild
+    from oracle import oracle as O
+    obuild.build_oracle()
+    points, xs, ys, zs, halo, dt, init = WORKLOADS[args.workload]
+    grid = (xs, ys, zs, halo, halo, halo)
+    if init == "blobs":
+        u = O.fill_blobs(grid, SEED, 8, 20.0)
+        v = u.copy()
+    else:
+        u = O.fill_uniform(grid, SEED, 0, -1e-3, 1e-3)
+        v = O.fill_uniform(grid, SEED + 1, 1, -1e-3, 1e-3)
+    s = np.zeros_like(u)
+    c0, c1, c2 = O.wave_constants(points, 1500.0, dt, 10.0)
+    src = (xs // 2, ys // 2, zs // 2)
+    # an even number of timed steps: the oracle moves the newest field back
+    # into `u` after an odd count, a copy that is not part of the update
+    timed = args.steps + (args.steps % 2)
+    amps = O.ricker_amps(0, args.warmup + timed + 1, dt)
+    O.iterate_wave(u, v, s, grid, points, args.warmup, c0, c1, c2, src=src, amps=amps)
+    t0 = time.perf_counter()
+    O.iterate_wave(u, v, s, grid, points, timed, c0, c1, c2, src=src,
+                   amps=amps[args.warmup:], fma=False)
+    el = time.perf_counter() - t0
+    value = xs * ys * zs * timed / el / 1e9
+    threads = host_threads()
+    kind = "reference" if O.ref_available(points) else "port"
+    sample = ("%d full leapfrog steps of %s on the CPU restatement (oracle), OpenMP %d threads"
+              % (timed, args.workload, threads))
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "Gpts/s + % of HBM roofline, 25-pt 1024^3: FP32 vs FP16-store at stated L2 err",
+        "value": value, "unit": "Gpts/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / timed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "points": points, "grid": [xs, ys, zs],
+                   "halo": halo, "form": "leapfrog wave", "dt": dt},
+        "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference has no wave form; its CPU path restated in C (oracle/st3d_oracle.c, "
+                "pinned bit-exact to the reference's mode R) runs the same update" +
+                ("" if kind == "port" else "; reference library also present"),
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gb300(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

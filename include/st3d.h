@@ -1,0 +1,208 @@
+/*
+ * st3d.h -- C ABI of the GB300 stencil3d library (libst3d.so).
+ *
+ * The library replaces the reference's host-CPU hot path: the time loop and
+ * traversal of iterators.cpp (ITERATE, iterators.h:6-29, selected by the
+ * ITERATE macro of config.h:55-65) and the per-point updates of
+ * stencil_{2,7,13,25}.h, on one GB300 GPU.  Every function returns an int
+ * status (ST3D_OK = 0); the reference itself returns no errors and exits on
+ * bad input (aux.cpp:16-69), so each entry point names the reference call it
+ * replaces and the checks it adds.
+ *
+ * Host arrays passed to the library use the reference layout
+ * (grid.cpp:20-24, stencils.h:5):
+ *     IDX(i,j,k) = ijk_ofs + k + j*jmult + i*imult,
+ *     jmult = zs + 2*zh, imult = jmult*(ys + 2*yh),
+ *     ijk_ofs = zh + yh*jmult + xh*imult,
+ * i the slowest (x) axis and k the contiguous (z) axis.  `real` is float for
+ * the F32, F16, BF16 and F16_HILO storages and double for F64
+ * (config.h:96-100).  The library keeps its own device layout and converts
+ * at upload and download.
+ *
+ * Plain pointers and sizes only: no C++ or framework types cross this ABI.
+ * One context per host thread; contexts share no mutable state.
+ */
+#ifndef ST3D_H
+#define ST3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ST3D_ABI_VERSION 1
+
+typedef enum st3d_status {
+  ST3D_OK = 0,
+  ST3D_ERR_INVALID = 1,     /* bad argument: size, halo, pointer, option */
+  ST3D_ERR_UNSUPPORTED = 2, /* well-formed request this library does not implement */
+  ST3D_ERR_CUDA = 3,        /* a CUDA runtime or driver call failed */
+  ST3D_ERR_NOMEM = 4,       /* device or pinned host allocation failed */
+  ST3D_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  ST3D_ERR_STATE = 6,       /* call out of order, e.g. iterate before upload */
+  ST3D_ERR_NODEVICE = 7     /* no CUDA device of compute capability 10.3 */
+} st3d_status;
+
+/* Update modes. */
+typedef enum st3d_mode {
+  /* The update the reference code computes (stencil_7.h:31-39,
+   * stencil_13.h:50-61, stencil_25.h:75-95, stencil_2.h:20-29):
+   *   v <- v - K*u + s*(coef0*u + sum c_{axis,r}*(u[-r] + u[+r]))
+   * (2 points: v <- coef0*(u + u[k+1])), u and s fixed between steps. */
+  ST3D_MODE_REF = 0,
+  /* Leapfrog acoustic wave (README.md:11-20):
+   *   v <- c0*u - v + c1*sum w_{axis,r}*(u[-r] + u[+r]) + c2*(s + a_n*delta_src)
+   * then u and v swap roles.  a_n is a Ricker wavelet at step n. */
+  ST3D_MODE_WAVE = 1
+} st3d_mode;
+
+typedef enum st3d_storage {
+  ST3D_F32 = 0,      /* float fields, float arithmetic */
+  ST3D_F64 = 1,      /* double fields, double arithmetic (config.h:96-97) */
+  ST3D_F16 = 2,      /* u,v,s stored as FP16 with a per-i-plane power-of-two scale, float arithmetic */
+  ST3D_BF16 = 3,     /* as F16 with bfloat16 storage */
+  ST3D_F16_HILO = 4  /* F16 plus a compensating low FP16 word for each field */
+} st3d_storage;
+
+typedef enum st3d_kernel {
+  ST3D_KERNEL_AUTO = 0,   /* the fastest kernel for the request */
+  ST3D_KERNEL_SIMPLE = 1, /* direct-load 2.5D streaming kernel (all storages) */
+  ST3D_KERNEL_TMA = 2     /* TMA-staged 2.5D streaming kernel (F32) */
+} st3d_kernel;
+
+typedef enum st3d_field {
+  ST3D_FIELD_U = 0,
+  ST3D_FIELD_V = 1,
+  ST3D_FIELD_S = 2
+} st3d_field;
+
+typedef enum st3d_fill_kind {
+  ST3D_FILL_CONST = 0,   /* every point, halos included: value a */
+  ST3D_FILL_UNIFORM = 1, /* every point, halos included: uniform [a, b) from the seeded counter hash */
+  ST3D_FILL_BLOBS = 2    /* interior: sum of (int)a Gaussian blobs of width b (seeded), halos 0 */
+} st3d_fill_kind;
+
+/* Grid geometry: the --xs/--ys/--zs/--xh/--yh/--zh values of main.cpp:125-144
+ * (s_grid xsize/ysize/zsize, xhalo/yhalo/zhalo, grid.h:39-41). */
+typedef struct st3d_grid_desc {
+  uint32_t xs, ys, zs; /* interior points along i (x), j (y), k (z) */
+  uint32_t xh, yh, zh; /* halo widths of the caller's host arrays; each >= the stencil radius */
+} st3d_grid_desc;
+
+typedef struct st3d_opts {
+  int32_t points;   /* 2, 7, 13 or 25 (config.h:35-38 STENCIL_SIZE) */
+  int32_t mode;     /* st3d_mode */
+  int32_t storage;  /* st3d_storage */
+  int32_t kernel;   /* st3d_kernel */
+  /* coef[0] = coef0 (2 points: the 0.5 factor), coef[1] = K,
+   * coef[2..5] = cx1..cx4, coef[6..9] = cy1..cy4, coef[10..13] = cz1..cz4.
+   * Mode W uses coef[2..13] as the neighbour weights w. */
+  double coef[14];
+  double c0, c1, c2;                 /* mode W constants */
+  int32_t src_i, src_j, src_k;       /* mode W point source (interior coordinates); src_i < 0: none */
+  int32_t pad0;
+  double src_f, src_t0, dt;          /* Ricker peak frequency [Hz], delay [s], time step [s] */
+  int32_t temporal_block;            /* mode W steps fused per pass: 1, 2 or 4 */
+  int32_t tile_j, tile_k;            /* CTA tile; 0 = automatic */
+  int32_t ichunk;                    /* planes per work unit along i; 0 = automatic */
+  int32_t reserved[8];
+} st3d_opts;
+
+typedef struct st3d_info {
+  uint64_t interior_points;   /* xs*ys*zs */
+  uint64_t device_bytes;      /* device memory held by the context */
+  uint64_t step;              /* steps taken since the last upload (mode W source clock) */
+  uint64_t launches;          /* kernel launches issued by st3d_iterate so far */
+  uint32_t nk, nj, ni;        /* device row pitch (elements), rows per plane, planes */
+  uint32_t pk, pj, pi;        /* device front pads (elements, rows, planes) */
+  int32_t kernel;             /* st3d_kernel actually used */
+  int32_t radius;             /* stencil radius */
+  double bytes_per_point;     /* algorithmic HBM bytes per point per step */
+  double flops_per_point;     /* reference FLOPS_PER_STENCIL (config.h:67-91) */
+  int32_t tile_j, tile_k, ichunk, temporal_block;
+  int32_t reserved[8];
+} st3d_info;
+
+typedef struct st3d_ctx st3d_ctx;
+
+/* ---- library ----------------------------------------------------------- */
+int st3d_abi_version(void);
+const char* st3d_status_string(int status);
+/* Detail of the last failure on the calling thread ("" if none). */
+const char* st3d_last_error(void);
+/* Current device: SM count, compute capability, total memory. */
+int st3d_device_info(int* sm_count, int* cc_major, int* cc_minor, size_t* total_bytes);
+
+/* Defaults: the reference's CONSTANTS_* for `points` (stencil_*.h; for F64
+ * storage the double products of config.h's real=double build), mode W
+ * weights 1 for 7 points (README.md:11-20) and stencil_*.h cx/cy/cz for 13 and
+ * 25, c = 1500 m/s, dx = 10 m, dt = 1 ms, 15 Hz Ricker with t0 = 1/f at the
+ * grid centre (set at st3d_create when src_i = -2). */
+int st3d_default_opts(int points, int mode, int storage, st3d_opts* opts);
+/* Mode W constants from physics: c1 = (vel*dt/dx)^2, c2 = dt^2,
+ * c0 = 2 - 2*c1*sum(w) (README.md:11-14 for w = 1). */
+int st3d_set_wave_physics(st3d_opts* opts, double vel, double dt, double dx);
+
+/* Validate a request and compute its device layout without touching a GPU:
+ * the same checks st3d_create makes before it allocates.  info->kernel is
+ * the kernel st3d_create would pick on a GB300 (the TMA kernel serves FP32
+ * with 7/13/25 points). */
+int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info);
+
+/* ---- context: replaces ITERATE's implicit state ------------------------ */
+/* Replaces s_grid construction (grid.cpp:9-48, main.cpp:201) and the field
+ * allocation of main.cpp:246-275: allocates the device fields of `grid`. */
+int st3d_create(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_ctx** ctx);
+int st3d_destroy(st3d_ctx* ctx);
+int st3d_get_info(const st3d_ctx* ctx, st3d_info* info);
+/* The context's CUDA stream (a cudaStream_t), for callers that order work. */
+int st3d_get_stream(const st3d_ctx* ctx, void** stream);
+
+/* Copy reference-layout host arrays in (NULL: leave that field).  u and v
+ * are copied with min(halo, 4) halo points per side (the stencil reads u's
+ * halo), s likewise.  Resets the mode W step clock to 0. */
+int st3d_upload(st3d_ctx* ctx, const void* v, const void* s, const void* u);
+/* Copy interior points out (halos of the host arrays are not written,
+ * as the reference never writes halos).  Mode W: u = newest field U^n,
+ * v = U^{n-1}.  NULL: skip. */
+int st3d_download(st3d_ctx* ctx, void* v, void* u);
+/* Replaces ITERATE(v,s,u,grid,prefetch,dups,iterations,cacheiter)
+ * (iterators.h:6-29, iterators.cpp:130-289) on device-resident fields:
+ * `iterations` steps, stream-ordered, asynchronous. */
+int st3d_iterate(st3d_ctx* ctx, uint32_t iterations);
+/* ITERATE drop-in on host arrays: upload v, s, u; iterate; download v (and,
+ * in mode W, u as well: u is then written although ITERATE declares it
+ * const); synchronize. */
+int st3d_iterate_host(st3d_ctx* ctx, void* v, const void* s, void* u, uint32_t iterations);
+int st3d_synchronize(st3d_ctx* ctx);
+
+/* Device-side initialisation of one field (st3d_fill_kind); replaces
+ * init_arrays (iterators.cpp:292-301) for ST3D_FILL_CONST. */
+int st3d_fill(st3d_ctx* ctx, int field, int kind, uint64_t seed, double a, double b);
+/* Replaces check() (iterators.cpp:304-325): counts interior points of v
+ * with |v - expected| > tol. */
+int st3d_check(st3d_ctx* ctx, double expected, double tol, uint64_t* errors);
+/* FP64 reductions over the interior of field fa of a against field fb of b
+ * (b may equal a; b = NULL: out[0] = sum a^2, out[2] = max|a|).
+ * out[0] = sum (a-b)^2, out[1] = sum b^2, out[2] = max|a-b|, out[3] = max|b|. */
+int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]);
+
+/* CUDA-event timing on the context's stream. */
+int st3d_timer_start(st3d_ctx* ctx);
+int st3d_timer_stop(st3d_ctx* ctx, float* ms);
+
+/* Pinned host memory for fast upload/download. */
+int st3d_host_alloc(size_t bytes, void** ptr);
+int st3d_host_free(void* ptr);
+
+/* The Ricker wavelet the mode W source uses: (1 - 2a) exp(-a),
+ * a = (pi f (t - t0))^2, evaluated on the host in double. */
+double st3d_ricker(double t, double f, double t0);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* ST3D_H */

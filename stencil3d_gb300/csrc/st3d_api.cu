@@ -1,0 +1,742 @@
+// st3d_api.cu -- the C ABI of libst3d (include/st3d.h): contexts, layout
+// conversion at the host boundary, kernel selection and the time loop.
+//
+// The reference drives its hot path through ITERATE (iterators.h:6-29) on
+// host arrays that main.cpp allocates (main.cpp:246-275) and initialises
+// (iterators.cpp:292-301).  Here a context owns the device copies of u, v,
+// s in the library's own layout (st3d_internal.h), converts from and to the
+// reference layout at upload and download, and runs the time loop on its own
+// CUDA stream.
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "st3d_internal.h"
+#include "st3d_tma.cuh"
+
+using namespace st3d;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? ST3D_ERR_NOMEM : ST3D_ERR_CUDA, "%s: %s (%s)", what,
+              cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define ST3D_CUDA(call)                                 \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+int elem_bytes(int storage) {
+  switch (storage) {
+    case ST3D_F32: return 4;
+    case ST3D_F64: return 8;
+    case ST3D_F16:
+    case ST3D_BF16:
+    case ST3D_F16_HILO: return 2;
+    default: return 0;
+  }
+}
+
+int host_elem_bytes(int storage) { return storage == ST3D_F64 ? 8 : 4; }
+
+}  // namespace
+
+namespace st3d {
+
+Layout make_layout(uint32_t xs, uint32_t ys, uint32_t zs, int eb) {
+  Layout L;
+  L.xs = xs; L.ys = ys; L.zs = zs;
+  L.pk = 128u / (uint32_t)eb;
+  L.pj = kMaxRadius;
+  L.pi = kMaxRadius;
+  const uint32_t need = L.pk + zs + L.pk;
+  L.nk = (need + L.pk - 1) / L.pk * L.pk;
+  L.nj = ys + 2 * L.pj;
+  L.ni = xs + 2 * L.pi;
+  return L;
+}
+
+template <typename C>
+Coefs<C> make_coefs(const st3d_opts& o) {
+  Coefs<C> c;
+  memset(&c, 0, sizeof c);
+  c.coef0 = (C)o.coef[0];
+  c.K = (C)o.coef[1];
+  c.c0 = (C)o.c0;
+  c.c1 = (C)o.c1;
+  c.c2 = (C)o.c2;
+  const int P = o.points;
+  for (int p = 0; p < npairs_of(P); ++p)
+    c.cf[p] = (C)o.coef[2 + 4 * pair_axis(P, p) + pair_r(P, p) - 1];
+  return c;
+}
+template Coefs<float> make_coefs<float>(const st3d_opts&);
+template Coefs<double> make_coefs<double>(const st3d_opts&);
+
+}  // namespace st3d
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct st3d_ctx {
+  st3d_grid_desc grid;
+  st3d_opts opts;
+  int R = 0;
+  int eb = 0;
+  Layout L;
+  Geom G;
+  void* fld[3] = {nullptr, nullptr, nullptr};  // [0],[1]: u/v pair, [2]: s
+  int cur = 0;                                 // mode W: fld[cur] is u
+  double* scratch = nullptr;                   // norms partials + result
+  unsigned long long* counter = nullptr;       // check()
+  uint32_t* dev_status = nullptr;
+  size_t scratch_doubles = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint64_t step = 0;
+  uint64_t launches = 0;
+  int kernel = ST3D_KERNEL_SIMPLE;
+  int ichunk = 64;
+  bool has_u = false, has_v = false, has_s = false;
+  int device = 0;
+  TmaPlan* tma = nullptr;
+  Coefs<float> cf32;
+  Coefs<double> cf64;
+  size_t bytes = 0;
+};
+
+namespace {
+
+int validate(const st3d_grid_desc* g, const st3d_opts* o) {
+  if (!g || !o) return fail(ST3D_ERR_INVALID, "null grid or options");
+  const int R = radius_of(o->points);
+  if (R < 0) return fail(ST3D_ERR_INVALID, "points must be 2, 7, 13 or 25 (got %d)", o->points);
+  if (o->mode != ST3D_MODE_REF && o->mode != ST3D_MODE_WAVE)
+    return fail(ST3D_ERR_INVALID, "unknown mode %d", o->mode);
+  if (elem_bytes(o->storage) == 0) return fail(ST3D_ERR_INVALID, "unknown storage %d", o->storage);
+  if (o->kernel < ST3D_KERNEL_AUTO || o->kernel > ST3D_KERNEL_TMA)
+    return fail(ST3D_ERR_INVALID, "unknown kernel %d", o->kernel);
+  if (g->xs < 1 || g->ys < 1 || g->zs < 1)
+    return fail(ST3D_ERR_INVALID, "grid sizes must be >= 1 (got %u x %u x %u)", g->xs, g->ys, g->zs);
+  if ((uint64_t)g->xs * g->ys * g->zs > (1ull << 36))
+    return fail(ST3D_ERR_INVALID, "grid of %llu points is beyond the library limit 2^36",
+                (unsigned long long)g->xs * g->ys * g->zs);
+  if (g->zs > (1u << 24) || g->ys > (1u << 24) || g->xs > (1u << 24))
+    return fail(ST3D_ERR_INVALID, "grid axis beyond 2^24 points");
+  // The stencil reads u up to R points beyond the interior on every axis
+  // (stencil_*.h neighbour loads); the 2-point stencil only reads k+1.
+  const uint32_t rx = o->points == 2 ? 0 : R, ry = rx, rz = R;
+  if (g->xh < rx || g->yh < ry || g->zh < rz)
+    return fail(ST3D_ERR_INVALID, "halo (%u,%u,%u) is narrower than the %d-point stencil needs (%u,%u,%u)",
+                g->xh, g->yh, g->zh, o->points, rx, ry, rz);
+  if (g->xh > 64 || g->yh > 64 || g->zh > 4096)
+    return fail(ST3D_ERR_INVALID, "halo (%u,%u,%u) too wide", g->xh, g->yh, g->zh);
+  if (o->mode == ST3D_MODE_WAVE && o->points == 2)
+    return fail(ST3D_ERR_UNSUPPORTED, "the 2-point stencil has no wave form (it is not a Laplacian)");
+  if (o->storage != ST3D_F32 && o->storage != ST3D_F64)
+    return fail(ST3D_ERR_UNSUPPORTED, "storage %d is not available in this build", o->storage);
+  if (o->kernel == ST3D_KERNEL_TMA && o->storage != ST3D_F32)
+    return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves FP32 storage only");
+  if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
+    return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves the 7/13/25-point stencils");
+  if (o->temporal_block != 0 && o->temporal_block != 1)
+    return fail(ST3D_ERR_UNSUPPORTED, "temporal blocking depth %d is not available in this build",
+                o->temporal_block);
+  if (o->mode == ST3D_MODE_WAVE && o->src_i >= 0 &&
+      ((uint32_t)o->src_i >= g->xs || o->src_j < 0 || (uint32_t)o->src_j >= g->ys ||
+       o->src_k < 0 || (uint32_t)o->src_k >= g->zs))
+    return fail(ST3D_ERR_INVALID, "source (%d,%d,%d) outside the interior", o->src_i, o->src_j,
+                o->src_k);
+  return ST3D_OK;
+}
+
+// TMA plan for an FP32 context: tile rows, stages, work units, grid.
+bool plan_tma(const st3d_ctx* c, int sm_count, int max_smem, TmaPlan* p) {
+  const int R = c->R;
+  p->radius = R;
+  p->tj = c->opts.tile_j > 0 ? c->opts.tile_j : 16;
+  p->nv = 3;
+  if (!tma_config_supported(p->tj, p->nv)) return false;
+  p->smem = tma_smem_bytes(p->tj, p->nv, R);
+  if ((int)p->smem > max_smem) return false;
+  const int per_sm = tma_blocks_per_sm(c->opts.points, c->opts.mode, p->tj, p->nv, p->smem);
+  if (per_sm < 1) return false;
+  p->ntj = (int)((c->L.ys + p->tj - 1) / p->tj);
+  p->ntk = (int)((c->L.zs + kTmaTK - 1) / kTmaTK);
+  const int ctas = sm_count * per_sm;
+  p->ichunk = c->opts.ichunk > 0 ? c->opts.ichunk
+                                 : tma_pick_ichunk((int)c->L.xs, p->ntj * p->ntk, ctas, R);
+  p->nti = (int)((c->L.xs + p->ichunk - 1) / p->ichunk);
+  p->units = p->ntj * p->ntk * p->nti;
+  p->grid = ctas < p->units ? ctas : p->units;
+  p->threads = (p->tj + 1) * 32;
+  return true;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+// Tensor map over one field buffer.  The extents stop where the stencil's
+// valid data stops (dim0 = row front pad + zs + `kext` halo points, dim1 =
+// front rows + ys + `jext` halo rows): box parts beyond them are out of bounds,
+// which TMA fills with zeros without reading memory, so partial edge tiles
+// cost no DRAM bytes.
+int encode_map(CUtensorMap* m, void* base, const Layout& L, uint32_t box_k, uint32_t box_j,
+               uint32_t kext, uint32_t jext) {
+  auto enc = get_encode();
+  if (!enc) return fail(ST3D_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  cuuint64_t dims[3] = {(cuuint64_t)L.pk + L.zs + kext, (cuuint64_t)L.pj + L.ys + jext, L.ni};
+  cuuint64_t strides[2] = {(cuuint64_t)L.nk * 4, (cuuint64_t)L.nk * L.nj * 4};
+  cuuint32_t box[3] = {box_k, box_j, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ST3D_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ST3D_OK;
+}
+
+void* u_ptr(st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->fld[c->cur] : c->fld[0]; }
+void* v_ptr(st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->fld[1 - c->cur] : c->fld[1]; }
+int u_index(const st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->cur : 0; }
+int v_index(const st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? 1 - c->cur : 1; }
+
+// Host (reference layout) <-> device (library layout) copy of one field.
+// `halo` points per side along each axis, capped by the host halos.
+int copy_field(st3d_ctx* c, void* dev, void* host, bool to_device, bool with_halo) {
+  const st3d_grid_desc& g = c->grid;
+  const int hb = host_elem_bytes(c->opts.storage);
+  const uint32_t hx = with_halo ? (g.xh < 4 ? g.xh : 4) : 0;
+  const uint32_t hy = with_halo ? (g.yh < 4 ? g.yh : 4) : 0;
+  const uint32_t hz = with_halo ? (g.zh < 4 ? g.zh : 4) : 0;
+  const size_t jmult = (size_t)g.zs + 2 * g.zh;
+  cudaMemcpy3DParms p;
+  memset(&p, 0, sizeof p);
+  cudaPitchedPtr hp = make_cudaPitchedPtr(host, jmult * hb, jmult, g.ys + 2 * g.yh);
+  cudaPitchedPtr dp = make_cudaPitchedPtr(dev, (size_t)c->L.nk * c->eb, c->L.nk, c->L.nj);
+  cudaPos hpos = make_cudaPos((g.zh - hz) * hb, g.yh - hy, g.xh - hx);
+  cudaPos dpos = make_cudaPos((c->L.pk - hz) * c->eb, c->L.pj - hy, c->L.pi - hx);
+  if (to_device) {
+    p.srcPtr = hp; p.srcPos = hpos; p.dstPtr = dp; p.dstPos = dpos;
+    p.kind = cudaMemcpyHostToDevice;
+  } else {
+    p.srcPtr = dp; p.srcPos = dpos; p.dstPtr = hp; p.dstPos = hpos;
+    p.kind = cudaMemcpyDeviceToHost;
+  }
+  p.extent = make_cudaExtent((g.zs + 2 * hz) * (size_t)hb, g.ys + 2 * hy, g.xs + 2 * hx);
+  ST3D_CUDA(cudaMemcpy3DAsync(&p, c->stream));
+  return ST3D_OK;
+}
+
+int check_device_status(st3d_ctx* c) {
+  uint32_t st = 0;
+  ST3D_CUDA(cudaMemcpyAsync(&st, c->dev_status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
+  ST3D_CUDA(cudaStreamSynchronize(c->stream));
+  if (st != kDevOk) {
+    ST3D_CUDA(cudaMemsetAsync(c->dev_status, 0, sizeof(uint32_t), c->stream));
+    return fail(ST3D_ERR_TIMEOUT, "a bounded device wait gave up (status %u)", st);
+  }
+  return ST3D_OK;
+}
+
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// library
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int st3d_abi_version(void) { return ST3D_ABI_VERSION; }
+
+const char* st3d_status_string(int s) {
+  switch (s) {
+    case ST3D_OK: return "ok";
+    case ST3D_ERR_INVALID: return "invalid argument";
+    case ST3D_ERR_UNSUPPORTED: return "unsupported";
+    case ST3D_ERR_CUDA: return "CUDA error";
+    case ST3D_ERR_NOMEM: return "out of memory";
+    case ST3D_ERR_TIMEOUT: return "device wait timed out";
+    case ST3D_ERR_STATE: return "call out of order";
+    case ST3D_ERR_NODEVICE: return "no GB300 (sm_103) device";
+    default: return "unknown status";
+  }
+}
+
+const char* st3d_last_error(void) { return g_last_error.c_str(); }
+
+int st3d_device_info(int* sm_count, int* cc_major, int* cc_minor, size_t* total_bytes) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(ST3D_ERR_NODEVICE, "no CUDA device visible (%s)", cudaGetErrorString(e));
+  }
+  int dev = 0;
+  ST3D_CUDA(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  ST3D_CUDA(cudaGetDeviceProperties(&prop, dev));
+  if (sm_count) *sm_count = prop.multiProcessorCount;
+  if (cc_major) *cc_major = prop.major;
+  if (cc_minor) *cc_minor = prop.minor;
+  if (total_bytes) *total_bytes = prop.totalGlobalMem;
+  return ST3D_OK;
+}
+
+int st3d_default_opts(int points, int mode, int storage, st3d_opts* o) {
+  if (!o) return fail(ST3D_ERR_INVALID, "null options");
+  memset(o, 0, sizeof *o);
+  o->points = points;
+  o->mode = mode;
+  o->storage = storage;
+  o->kernel = ST3D_KERNEL_AUTO;
+  o->temporal_block = 1;
+  o->src_i = -2;  // grid centre, resolved at st3d_create
+  o->src_f = 15.0;
+  o->src_t0 = 1.0 / 15.0;
+  const bool dbl = storage == ST3D_F64;
+  // The reference's CONSTANTS_* (stencil_7.h:4-8, stencil_13.h:4-22,
+  // stencil_25.h:20-34).  The y/z coefficients are products formed in the
+  // type of `real` (config.h:96-100): float products widened for float
+  // storage, double products of the widened literals for double storage.
+  auto mul = [dbl](float a, float b) -> double {
+    return dbl ? (double)a * (double)b : (double)(a * b);
+  };
+  double* c = o->coef;
+  if (points == 2) {
+    c[0] = 0.5f;
+  } else if (points == 7) {
+    c[0] = 1.5f; c[1] = 3.5f;
+    c[2] = 0.5f; c[6] = 0.5f; c[10] = 0.5f;
+  } else if (points == 13) {
+    const float cx[2] = {0.3f, 0.2f};
+    c[0] = 1.5f; c[1] = 3.5f;
+    for (int r = 0; r < 2; ++r) {
+      c[2 + r] = cx[r];
+      c[6 + r] = mul(cx[r], 1.1f);
+      c[10 + r] = mul(cx[r], 0.9f);
+    }
+  } else if (points == 25) {
+    const float cx[4] = {0.4f, 0.3f, 0.2f, 0.1f};
+    c[0] = 1.25f; c[1] = 6.25f;
+    for (int r = 0; r < 4; ++r) {
+      c[2 + r] = cx[r];
+      c[6 + r] = mul(cx[r], 1.1f);
+      c[10 + r] = mul(cx[r], 0.9f);
+    }
+  } else {
+    return fail(ST3D_ERR_INVALID, "points must be 2, 7, 13 or 25 (got %d)", points);
+  }
+  if (mode == ST3D_MODE_WAVE && points == 7) {
+    // README.md:11-20: unit neighbour weights for the 7-point wave form.
+    c[2] = c[6] = c[10] = 1.0;
+  }
+  if (mode == ST3D_MODE_WAVE) {
+    c[0] = c[1] = 0.0;
+    st3d_set_wave_physics(o, 1500.0, 1e-3, 10.0);
+  }
+  return ST3D_OK;
+}
+
+int st3d_set_wave_physics(st3d_opts* o, double vel, double dt, double dx) {
+  if (!o || !(vel > 0) || !(dt > 0) || !(dx > 0))
+    return fail(ST3D_ERR_INVALID, "wave physics needs positive velocity, dt and dx");
+  const double c1 = (vel * dt / dx) * (vel * dt / dx);
+  double wsum = 0.0;
+  for (int m = 2; m < 14; ++m) wsum += o->coef[m];
+  o->c0 = 2.0 - 2.0 * c1 * wsum;
+  o->c1 = c1;
+  o->c2 = dt * dt;
+  o->dt = dt;
+  return ST3D_OK;
+}
+
+double st3d_ricker(double t, double f, double t0) {
+  const double pf = 3.14159265358979323846 * f * (t - t0);
+  const double a = pf * pf;
+  return (1.0 - 2.0 * a) * std::exp(-a);
+}
+
+int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info) {
+  if (!info) return fail(ST3D_ERR_INVALID, "null info");
+  int rc = validate(grid, opts);
+  if (rc != ST3D_OK) return rc;
+  memset(info, 0, sizeof *info);
+  const int eb = elem_bytes(opts->storage);
+  const Layout L = make_layout(grid->xs, grid->ys, grid->zs, eb);
+  const int R = radius_of(opts->points);
+  info->interior_points = (uint64_t)grid->xs * grid->ys * grid->zs;
+  info->device_bytes = 3 * L.elems() * eb;
+  info->nk = L.nk; info->nj = L.nj; info->ni = L.ni;
+  info->pk = L.pk; info->pj = L.pj; info->pi = L.pi;
+  info->radius = R;
+  info->bytes_per_point = (opts->points == 2 ? 2.0 : 4.0) * eb;
+  info->flops_per_point = opts->points == 2 ? 2 : opts->points == 7 ? 12 : opts->points == 13 ? 29 : 41;
+  const int tj = opts->tile_j > 0 ? opts->tile_j : 16;
+  const bool tma = opts->storage == ST3D_F32 && opts->points != 2 &&
+                   opts->kernel != ST3D_KERNEL_SIMPLE && tma_config_supported(tj, 3);
+  info->kernel = tma ? ST3D_KERNEL_TMA : ST3D_KERNEL_SIMPLE;
+  info->tile_j = tma ? tj : 0;
+  info->tile_k = tma ? kTmaTK : 0;
+  info->ichunk = opts->ichunk > 0 ? opts->ichunk : (tma ? 128 : 64);
+  info->temporal_block = opts->temporal_block > 0 ? opts->temporal_block : 1;
+  return ST3D_OK;
+}
+
+int st3d_create(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_ctx** out) {
+  if (!out) return fail(ST3D_ERR_INVALID, "null context pointer");
+  *out = nullptr;
+  int rc = validate(grid, opts);
+  if (rc != ST3D_OK) return rc;
+  int sm = 0, ccM = 0, ccm = 0;
+  size_t total = 0;
+  rc = st3d_device_info(&sm, &ccM, &ccm, &total);
+  if (rc != ST3D_OK) return rc;
+  if (ccM != 10 || ccm != 3)
+    return fail(ST3D_ERR_NODEVICE, "device has compute capability %d.%d; this library is built for sm_103a",
+                ccM, ccm);
+  st3d_ctx* c = new (std::nothrow) st3d_ctx();
+  if (!c) return fail(ST3D_ERR_NOMEM, "host allocation failed");
+  c->grid = *grid;
+  c->opts = *opts;
+  if (c->opts.temporal_block == 0) c->opts.temporal_block = 1;
+  c->R = radius_of(opts->points);
+  c->eb = elem_bytes(opts->storage);
+  c->L = make_layout(grid->xs, grid->ys, grid->zs, c->eb);
+  c->G = geom_of(c->L);
+  cudaGetDevice(&c->device);
+  if (c->opts.mode == ST3D_MODE_WAVE && c->opts.src_i == -2) {
+    c->opts.src_i = (int)grid->xs / 2;
+    c->opts.src_j = (int)grid->ys / 2;
+    c->opts.src_k = (int)grid->zs / 2;
+  }
+  c->cf32 = make_coefs<float>(c->opts);
+  c->cf64 = make_coefs<double>(c->opts);
+  auto cleanup = [c](int status) {
+    st3d_destroy(c);
+    return status;
+  };
+  const size_t fbytes = c->L.elems() * c->eb;
+  for (int f = 0; f < 3; ++f) {
+    cudaError_t e = cudaMalloc(&c->fld[f], fbytes);
+    if (e != cudaSuccess) {
+      c->fld[f] = nullptr;
+      cudaGetLastError();
+      return cleanup(fail(ST3D_ERR_NOMEM, "cudaMalloc of %zu bytes for field %d failed", fbytes, f));
+    }
+    c->bytes += fbytes;
+  }
+  c->scratch_doubles = 4 * (size_t)norms_blocks(c->G) + 8;
+  if (cudaMalloc(&c->scratch, c->scratch_doubles * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->counter, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&c->dev_status, sizeof(uint32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(fail(ST3D_ERR_NOMEM, "cudaMalloc of scratch failed"));
+  }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(fail(ST3D_ERR_CUDA, "stream/event creation failed"));
+  }
+  for (int f = 0; f < 3; ++f)
+    if (cudaMemsetAsync(c->fld[f], 0, fbytes, c->stream) != cudaSuccess)
+      return cleanup(fail(ST3D_ERR_CUDA, "cudaMemsetAsync failed"));
+  cudaMemsetAsync(c->dev_status, 0, sizeof(uint32_t), c->stream);
+
+  // kernel choice
+  c->kernel = ST3D_KERNEL_SIMPLE;
+  c->ichunk = c->opts.ichunk > 0 ? c->opts.ichunk : 64;
+  if (c->opts.storage == ST3D_F32 && c->opts.points != 2 && c->opts.kernel != ST3D_KERNEL_SIMPLE) {
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    TmaPlan* p = new (std::nothrow) TmaPlan();
+    if (p && plan_tma(c, sm, max_smem, p)) {
+      int ok = ST3D_OK;
+      for (int f = 0; f < 3 && ok == ST3D_OK; ++f) {
+        ok = encode_map(&p->umap[f], c->fld[f], c->L, kTmaUKW, p->tj + 2 * c->R, kTmaKHalo,
+                        c->L.pj);
+        if (ok == ST3D_OK) ok = encode_map(&p->vmap[f], c->fld[f], c->L, kTmaTK, p->tj, 0, 0);
+      }
+      if (ok == ST3D_OK) {
+        c->tma = p;
+        c->kernel = ST3D_KERNEL_TMA;
+      } else {
+        delete p;
+        if (c->opts.kernel == ST3D_KERNEL_TMA) return cleanup(ok);
+      }
+    } else {
+      delete p;
+      if (c->opts.kernel == ST3D_KERNEL_TMA)
+        return cleanup(fail(ST3D_ERR_UNSUPPORTED,
+                            "the TMA kernel cannot run with this configuration"));
+    }
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return cleanup(fail(ST3D_ERR_CUDA, "initial synchronize failed"));
+  *out = c;
+  return ST3D_OK;
+}
+
+int st3d_destroy(st3d_ctx* c) {
+  if (!c) return ST3D_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int f = 0; f < 3; ++f)
+    if (c->fld[f]) cudaFree(c->fld[f]);
+  if (c->scratch) cudaFree(c->scratch);
+  if (c->counter) cudaFree(c->counter);
+  if (c->dev_status) cudaFree(c->dev_status);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c->tma;
+  delete c;
+  return ST3D_OK;
+}
+
+int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
+  if (!c || !info) return fail(ST3D_ERR_INVALID, "null argument");
+  memset(info, 0, sizeof *info);
+  info->interior_points = (uint64_t)c->grid.xs * c->grid.ys * c->grid.zs;
+  info->device_bytes = c->bytes;
+  info->step = c->step;
+  info->launches = c->launches;
+  info->nk = c->L.nk; info->nj = c->L.nj; info->ni = c->L.ni;
+  info->pk = c->L.pk; info->pj = c->L.pj; info->pi = c->L.pi;
+  info->kernel = c->kernel;
+  info->radius = c->R;
+  // Algorithmic bytes per point per step: read u, v, s and write v
+  // (config.h:76,82,88 MEM_BYTES_PER_STENCIL counts the 3 streams + 1
+  // store); 2 points read u and write v (config.h:70).
+  info->bytes_per_point = (c->opts.points == 2 ? 2.0 : 4.0) * c->eb;
+  info->flops_per_point = c->opts.points == 2 ? 2 : c->opts.points == 7 ? 12 : c->opts.points == 13 ? 29 : 41;
+  info->tile_j = c->tma ? c->tma->tj : 0;
+  info->tile_k = c->tma ? kTmaTK : 0;
+  info->ichunk = c->tma ? c->tma->ichunk : c->ichunk;
+  info->temporal_block = c->opts.temporal_block;
+  return ST3D_OK;
+}
+
+int st3d_get_stream(const st3d_ctx* c, void** s) {
+  if (!c || !s) return fail(ST3D_ERR_INVALID, "null argument");
+  *s = (void*)c->stream;
+  return ST3D_OK;
+}
+
+int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  int rc;
+  if (u) {
+    if ((rc = copy_field(c, u_ptr(c), const_cast<void*>(u), true, true)) != ST3D_OK) return rc;
+    c->has_u = true;
+  }
+  if (v) {
+    if ((rc = copy_field(c, v_ptr(c), const_cast<void*>(v), true, true)) != ST3D_OK) return rc;
+    c->has_v = true;
+  }
+  if (s) {
+    if ((rc = copy_field(c, c->fld[2], const_cast<void*>(s), true, true)) != ST3D_OK) return rc;
+    c->has_s = true;
+  }
+  c->step = 0;
+  return ST3D_OK;
+}
+
+int st3d_download(st3d_ctx* c, void* v, void* u) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  int rc;
+  if (v && (rc = copy_field(c, v_ptr(c), v, false, false)) != ST3D_OK) return rc;
+  if (u && (rc = copy_field(c, u_ptr(c), u, false, false)) != ST3D_OK) return rc;
+  ST3D_CUDA(cudaStreamSynchronize(c->stream));
+  return ST3D_OK;
+}
+
+int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  if (!(c->has_u && c->has_v && c->has_s))
+    return fail(ST3D_ERR_STATE, "upload or fill u, v and s before iterating");
+  const bool wave = c->opts.mode == ST3D_MODE_WAVE;
+  for (uint32_t n = 0; n < iterations; ++n) {
+    Source src;
+    src.i = -1; src.j = -1; src.k = -1; src.amp = 0.0f; src.amp_d = 0.0;
+    if (wave && c->opts.src_i >= 0) {
+      src.i = c->opts.src_i; src.j = c->opts.src_j; src.k = c->opts.src_k;
+      src.amp_d = st3d_ricker((double)c->step * c->opts.dt, c->opts.src_f, c->opts.src_t0);
+      src.amp = (float)src.amp_d;
+    }
+    cudaError_t e;
+    if (c->kernel == ST3D_KERNEL_TMA) {
+      e = launch_tma(*c->tma, c->opts.points, c->opts.mode, c->G, c->cf32, (float*)v_ptr(c),
+                     u_index(c), v_index(c), 2, src, c->dev_status, c->stream);
+    } else {
+      const void* cf = c->opts.storage == ST3D_F64 ? (const void*)&c->cf64 : (const void*)&c->cf32;
+      e = launch_simple(c->opts.points, c->opts.mode, c->opts.storage, c->G, cf, v_ptr(c),
+                        u_ptr(c), c->fld[2], src, c->ichunk, c->stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "stencil kernel launch");
+    ++c->launches;
+    ++c->step;
+    if (wave) c->cur ^= 1;
+  }
+  return ST3D_OK;
+}
+
+int st3d_synchronize(st3d_ctx* c) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  ST3D_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->kernel == ST3D_KERNEL_TMA) return check_device_status(c);
+  return ST3D_OK;
+}
+
+int st3d_iterate_host(st3d_ctx* c, void* v, const void* s, void* u, uint32_t iterations) {
+  if (!c || !v || !s || !u) return fail(ST3D_ERR_INVALID, "null argument");
+  int rc = st3d_upload(c, v, s, u);
+  if (rc == ST3D_OK) rc = st3d_iterate(c, iterations);
+  if (rc == ST3D_OK)
+    rc = st3d_download(c, v, c->opts.mode == ST3D_MODE_WAVE ? u : nullptr);
+  if (rc == ST3D_OK) rc = st3d_synchronize(c);
+  return rc;
+}
+
+int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double b) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  if (field < ST3D_FIELD_U || field > ST3D_FIELD_S) return fail(ST3D_ERR_INVALID, "bad field %d", field);
+  if (kind < ST3D_FILL_CONST || kind > ST3D_FILL_BLOBS) return fail(ST3D_ERR_INVALID, "bad fill kind %d", kind);
+  void* dst = field == ST3D_FIELD_U ? u_ptr(c) : field == ST3D_FIELD_V ? v_ptr(c) : c->fld[2];
+  double bp[4 * 16];
+  int nb = 0;
+  if (kind == ST3D_FILL_BLOBS) {
+    nb = (int)a;
+    if (nb < 0 || nb > 16) return fail(ST3D_ERR_INVALID, "1..16 blobs (got %d)", nb);
+    if (!(b > 0)) return fail(ST3D_ERR_INVALID, "blob width must be positive");
+    // Same parameter stream as the seeded host generator: draw n of
+    // splitmix64(seed + (n+1)*golden), top 24 bits.
+    auto mix64 = [](uint64_t z) {
+      z ^= z >> 30; z *= 0xBF58476D1CE4E5B9ULL;
+      z ^= z >> 27; z *= 0x94D049BB133111EBULL;
+      z ^= z >> 31;
+      return z;
+    };
+    auto unit = [&](unsigned n) {
+      return (double)(mix64(seed + (uint64_t)(n + 1) * 0x9E3779B97F4A7C15ULL) >> 40) *
+             (1.0 / 16777216.0);
+    };
+    for (int q = 0; q < nb; ++q) {
+      bp[4 * q + 0] = unit(4 * q + 0) * c->grid.xs;
+      bp[4 * q + 1] = unit(4 * q + 1) * c->grid.ys;
+      bp[4 * q + 2] = unit(4 * q + 2) * c->grid.zs;
+      bp[4 * q + 3] = 2.0 * unit(4 * q + 3) - 1.0;
+    }
+  }
+  cudaError_t e = launch_fill(c->opts.storage, c->L, dst, kind, seed, (unsigned)field, a, b, bp, nb,
+                              c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "fill kernel launch");
+  if (field == ST3D_FIELD_U) c->has_u = true;
+  if (field == ST3D_FIELD_V) c->has_v = true;
+  if (field == ST3D_FIELD_S) c->has_s = true;
+  c->step = 0;
+  return ST3D_OK;
+}
+
+int st3d_check(st3d_ctx* c, double expected, double tol, uint64_t* errors) {
+  if (!c || !errors) return fail(ST3D_ERR_INVALID, "null argument");
+  ST3D_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned long long), c->stream));
+  cudaError_t e = launch_check(c->opts.storage, c->G, v_ptr(c), expected, tol, c->counter, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "check kernel launch");
+  unsigned long long n = 0;
+  ST3D_CUDA(cudaMemcpyAsync(&n, c->counter, sizeof n, cudaMemcpyDeviceToHost, c->stream));
+  ST3D_CUDA(cudaStreamSynchronize(c->stream));
+  *errors = n;
+  return ST3D_OK;
+}
+
+int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]) {
+  if (!a || !out) return fail(ST3D_ERR_INVALID, "null argument");
+  if (b && (b->grid.xs != a->grid.xs || b->grid.ys != a->grid.ys || b->grid.zs != a->grid.zs))
+    return fail(ST3D_ERR_INVALID, "norms need equal interior sizes");
+  auto fptr = [](st3d_ctx* c, int f) -> void* {
+    return f == ST3D_FIELD_U ? u_ptr(c) : f == ST3D_FIELD_V ? v_ptr(c) : c->fld[2];
+  };
+  if (fa < 0 || fa > 2 || (b && (fb < 0 || fb > 2))) return fail(ST3D_ERR_INVALID, "bad field");
+  if (b && b->stream != a->stream) ST3D_CUDA(cudaStreamSynchronize(b->stream));
+  const int nb = norms_blocks(a->G);
+  cudaError_t e = launch_norms(a->opts.storage, a->G, fptr(a, fa), b ? b->opts.storage : 0,
+                               b ? b->G : a->G, b ? fptr(b, fb) : nullptr, a->scratch, nb,
+                               a->scratch + 4 * (size_t)nb, a->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "norms kernel launch");
+  double h[4];
+  ST3D_CUDA(cudaMemcpyAsync(h, a->scratch + 4 * (size_t)nb, sizeof h, cudaMemcpyDeviceToHost, a->stream));
+  ST3D_CUDA(cudaStreamSynchronize(a->stream));
+  if (!b) {  // energy form: sum a^2 and max |a|
+    out[0] = h[0]; out[1] = 0.0; out[2] = h[2]; out[3] = 0.0;
+  } else {
+    for (int q = 0; q < 4; ++q) out[q] = h[q];
+  }
+  return ST3D_OK;
+}
+
+int st3d_timer_start(st3d_ctx* c) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  ST3D_CUDA(cudaEventRecord(c->ev0, c->stream));
+  return ST3D_OK;
+}
+
+int st3d_timer_stop(st3d_ctx* c, float* ms) {
+  if (!c || !ms) return fail(ST3D_ERR_INVALID, "null argument");
+  ST3D_CUDA(cudaEventRecord(c->ev1, c->stream));
+  ST3D_CUDA(cudaEventSynchronize(c->ev1));
+  ST3D_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev1));
+  return ST3D_OK;
+}
+
+int st3d_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return fail(ST3D_ERR_INVALID, "null pointer");
+  *ptr = nullptr;
+  cudaError_t e = cudaMallocHost(ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ST3D_ERR_NOMEM, "cudaMallocHost(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return ST3D_OK;
+}
+
+int st3d_host_free(void* ptr) {
+  if (ptr) ST3D_CUDA(cudaFreeHost(ptr));
+  return ST3D_OK;
+}
+
+}  // extern "C"

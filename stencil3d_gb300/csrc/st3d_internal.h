@@ -1,0 +1,128 @@
+// st3d_internal.h -- shared declarations of the libst3d CUDA sources.
+//
+// Device layout of one field (all storages):
+//   element (i,j,k) of the interior, 0 <= i < xs etc., lives at
+//   ((i + pi)*nj + (j + pj))*nk + (k + pk)
+//   pk = 128 bytes of front pad per row, so every interior row starts on a
+//   128-byte boundary; nk rounds pk + zs + pk up to a multiple of pk, so each
+//   row pitch is a multiple of 128 bytes (TMA strides must be multiples of
+//   16 bytes, coalesced rows want 128).
+//   pj = pi = 4 rows / planes: the widest stencil radius (25 points, r = 4).
+// The halo points the stencil reads are the caller's halo values, copied at
+// upload; the rest of the padding is zero.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "st3d.h"
+
+namespace st3d {
+
+constexpr int kMaxRadius = 4;
+
+struct Layout {
+  uint32_t xs, ys, zs;
+  uint32_t pk, pj, pi;
+  uint32_t nk, nj, ni;
+  size_t elems() const { return (size_t)nk * nj * ni; }
+  long long sj() const { return (long long)nk; }
+  long long si() const { return (long long)nk * nj; }
+  // offset of interior point (0,0,0)
+  long long org() const { return (long long)pi * si() + (long long)pj * sj() + pk; }
+};
+
+Layout make_layout(uint32_t xs, uint32_t ys, uint32_t zs, int elem_bytes);
+
+inline int radius_of(int points) {
+  switch (points) {
+    case 2: return 1;
+    case 7: return 1;
+    case 13: return 2;
+    case 25: return 4;
+    default: return -1;
+  }
+}
+
+// Neighbour-pair evaluation order of the reference sums (axis 0 = i/x,
+// 1 = j/y, 2 = k/z):
+//   7 : x1 y1 z1                 stencil_7.h:20
+//   13: z2 z1 y2 y1 x2 x1        stencil_13.h:40-43
+//   25: z4..z1 y4..y1 x4..x1     stencil_25.h:64-67
+__host__ __device__ constexpr int npairs_of(int P) { return P == 7 ? 3 : P == 13 ? 6 : P == 25 ? 12 : 0; }
+__host__ __device__ constexpr int pair_axis(int P, int p) {
+  return P == 7 ? p : 2 - p / (P == 13 ? 2 : 4);
+}
+__host__ __device__ constexpr int pair_r(int P, int p) {
+  return P == 7 ? 1 : (P == 13 ? 2 - (p % 2) : 4 - (p % 4));
+}
+
+// Coefficients in the compute type C, pair coefficients already in the
+// evaluation order above.
+template <typename C>
+struct Coefs {
+  C coef0, K;      // mode R
+  C c0, c1, c2;    // mode W
+  C cf[12];
+};
+
+template <typename C>
+Coefs<C> make_coefs(const st3d_opts& o);
+
+// Geometry passed to kernels by value.
+struct Geom {
+  int xs, ys, zs;
+  int pk, pj, pi;
+  long long sj, si, org;
+};
+
+inline Geom geom_of(const Layout& L) {
+  Geom g;
+  g.xs = (int)L.xs; g.ys = (int)L.ys; g.zs = (int)L.zs;
+  g.pk = (int)L.pk; g.pj = (int)L.pj; g.pi = (int)L.pi;
+  g.sj = L.sj(); g.si = L.si(); g.org = L.org();
+  return g;
+}
+
+// Mode W point source for one step.
+struct Source {
+  int i, j, k;   // interior coordinates; i < 0: none
+  float amp;     // s is replaced by s + amp at the source point
+  double amp_d;  // the same amplitude for double storage
+};
+
+// Device status word values set by bounded waits.
+enum DeviceStatus : uint32_t {
+  kDevOk = 0,
+  kDevTimeoutFull = 1,
+  kDevTimeoutEmpty = 2,
+};
+
+// ---- kernel launchers (st3d_kernels_*.cu) --------------------------------
+// All launch on `stream` and return the cudaGetLastError() of the launch.
+cudaError_t launch_simple(int points, int mode, int storage, const Geom& g, const void* coefs,
+                          void* v, const void* u, const void* s, const Source& src,
+                          int ichunk, cudaStream_t stream);
+
+struct TmaPlan;
+// ubuf/vbuf/sbuf select the tensor maps of the field buffers holding u, v, s.
+cudaError_t launch_tma(const TmaPlan& plan, int points, int mode, const Geom& g, const Coefs<float>& cf,
+                       float* v, int ubuf, int vbuf, int sbuf, const Source& src, uint32_t* dev_status,
+                       cudaStream_t stream);
+bool tma_config_supported(int tj, int nv);
+// Resident CTAs per SM of the TMA kernel for this configuration (0: cannot run).
+int tma_blocks_per_sm(int points, int mode, int tj, int nv, size_t smem);
+
+cudaError_t launch_fill(int storage, const Layout& L, void* dst, int kind, uint64_t seed,
+                        unsigned field, double a, double b, const double* blob_params, int nblobs,
+                        cudaStream_t stream);
+cudaError_t launch_check(int storage, const Geom& g, const void* v, double expected, double tol,
+                         unsigned long long* counter, cudaStream_t stream);
+// Two-pass FP64 reduction: partials of `nblocks` blocks in scratch, then one block.
+cudaError_t launch_norms(int sa, const Geom& ga, const void* a, int sb, const Geom& gb, const void* b,
+                         double* scratch, int nblocks, double* out_dev, cudaStream_t stream);
+int norms_blocks(const Geom& g);
+
+}  // namespace st3d

@@ -1,0 +1,325 @@
+// st3d_kernels_tma.cu -- the FP32 hot path: a TMA-staged 2.5D streaming
+// stencil kernel for sm_103a.
+//
+// Replaces the traversal and per-point update of the reference's ITERATE
+// (iterators.cpp:130-289 with stencil_{7,13,25}.h) for one time step.
+//
+// Work decomposition.  A work unit is a tile of TJ rows (j) x 128 points (k)
+// and a chunk of `ichunk` planes along i, the slowest axis.  A persistent
+// grid of at most (#SMs x resident CTAs) CTAs takes units round robin; the
+// unit order runs over all tiles of one i-chunk before the next, so CTAs
+// working at the same time hold neighbouring tiles and their halo rows meet
+// in L2.
+//
+// Inside a CTA (warp specialised):
+//   - one producer warp: lane 0 streams planes in with 3-D tiled TMA loads,
+//     one pipeline stage per plane step: the u tile of plane i+R with its
+//     halo (TJ+2R rows x 136 floats: 4 floats = 16 bytes either side along
+//     k keep every TMA x-coordinate 16-byte aligned), and the v and s tiles
+//     of plane i.  A stage completes on its `full` mbarrier by transaction
+//     bytes; the producer reuses a stage once all consumer warps arrived on
+//     its `empty` mbarrier.
+//   - TJ consumer warps, one per row; each lane owns 4 consecutive k points
+//     (one float4).  Along i a lane keeps u(i-R .. i+R) of its 4 points in a
+//     register queue of 2R+1 float4 whose slot for local step n is n mod
+//     (2R+1): the step loop is unrolled 2R+1 times so every queue index is a
+//     compile-time constant and nothing is shifted.  j neighbours come from
+//     the shared-memory u tile of plane i (kept for R+1 stages: the u ring has
+//     nv+R slots), k neighbours from the same row (128-bit shared loads of
+//     the left and right float4).  v and s come from their stage slots; the
+//     new v leaves with a 128-bit coalesced store.
+// Every wait is bounded (mbar_wait_bounded): on timeout the kernel records
+// the reason in a device status word and returns, so a broken pipeline ends
+// as an error code instead of a hung GPU.
+//
+// Arithmetic: the same operation sequence as the direct-load kernel and the
+// oracle's fma flavour (see st3d_kernels_simple.cu).
+#include "st3d_internal.h"
+#include "st3d_tma.cuh"
+
+namespace st3d {
+
+namespace {
+
+template <int P>
+struct RadiusOf {
+  static constexpr int value = (P == 25) ? 4 : (P == 13) ? 2 : 1;
+};
+
+template <int P, int MODE, int TJ, int NV>
+__global__ void __launch_bounds__((TJ + 1) * 32, 1)
+    k_tma(const __grid_constant__ CUtensorMap umap, const __grid_constant__ CUtensorMap vmap,
+          const __grid_constant__ CUtensorMap smap, Geom g, Coefs<float> cf,
+          float* __restrict__ vout, int ntk, int ntjk, int ichunk, int units, Source src,
+          uint64_t timeout_ns, uint32_t* __restrict__ status) {
+  constexpr int R = RadiusOf<P>::value;
+  constexpr int QN = 2 * R + 1;
+  constexpr int NU = NV + R;
+  constexpr int NP = npairs_of(P);
+  constexpr int TK = kTmaTK;
+  constexpr int UKW = kTmaUKW;
+  // Slots start on 128-byte boundaries (TMA shared-memory destinations);
+  // the transaction counts are the boxes' bytes.
+  constexpr int USLOT = (UKW * (TJ + 2 * R) + 31) / 32 * 32;  // floats
+  constexpr int VSLOT = TK * TJ;                              // floats
+  constexpr uint32_t UBYTES = UKW * (TJ + 2 * R) * 4;
+  constexpr uint32_t VBYTES = VSLOT * 4;
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* ur = reinterpret_cast<float*>(smem_raw);
+  float* vr = ur + NU * USLOT;
+  float* sr = vr + NV * VSLOT;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sr + NV * VSLOT);
+  uint64_t* empty = full + NV;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < NV; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], TJ);
+    }
+    fence_barrier_init();
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+
+  if (warp == TJ) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      tma_prefetch_desc(&umap);
+      tma_prefetch_desc(&vmap);
+      tma_prefetch_desc(&smap);
+      uint32_t h = 0;
+      bool ok = true;
+      for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
+        const int ic = unit / ntjk;
+        const int rem = unit - ic * ntjk;
+        const int jt = rem / ntk;
+        const int kt = rem - jt * ntk;
+        const int k0 = kt * TK, j0 = jt * TJ;
+        const int ia = ic * ichunk;
+        const int ib = min(ia + ichunk, g.xs);
+        const int nsteps = (ib - ia) + 2 * R;
+        for (int n = 0; n < nsteps; ++n, ++h) {
+          const int stage = (int)(h % NV);
+          if (h >= (uint32_t)NV) {
+            if (!mbar_wait_bounded(&empty[stage], ((h / NV) - 1) & 1u, timeout_ns)) {
+              atomicExch(status, (uint32_t)kDevTimeoutEmpty);
+              ok = false;
+              break;
+            }
+          }
+          const bool has_vs = n >= 2 * R;
+          mbar_arrive_expect_tx(&full[stage], UBYTES + (has_vs ? 2 * VBYTES : 0u));
+          const int p = ia - R + n;  // u plane loaded at this step
+          tma_load_3d(ur + (h % NU) * USLOT, &umap, &full[stage], g.pk + k0 - kTmaKHalo,
+                      g.pj + j0 - R, g.pi + p);
+          if (has_vs) {
+            const int i = ia + n - 2 * R;
+            tma_load_3d(vr + stage * VSLOT, &vmap, &full[stage], g.pk + k0, g.pj + j0, g.pi + i);
+            tma_load_3d(sr + stage * VSLOT, &smap, &full[stage], g.pk + k0, g.pj + j0, g.pi + i);
+          }
+        }
+      }
+      // Leave no copy in flight: wait for the stages issued last.
+      for (uint32_t m = (h > (uint32_t)NV ? h - NV : 0u); m < h; ++m)
+        (void)mbar_wait_bounded(&full[m % NV], (m / NV) & 1u, timeout_ns);
+    }
+    return;
+  }
+
+  // ---------------- consumers ----------------
+  const int r = warp;
+  uint32_t h = 0;
+  float4 q[QN];
+  for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+    const int ic = unit / ntjk;
+    const int rem = unit - ic * ntjk;
+    const int jt = rem / ntk;
+    const int kt = rem - jt * ntk;
+    const int j = jt * TJ + r;
+    const int k = kt * TK + 4 * lane;
+    const int ia = ic * ichunk;
+    const int ib = min(ia + ichunk, g.xs);
+    const int nsteps = (ib - ia) + 2 * R;
+    const bool row_ok = j < g.ys;
+    float* vrow = vout + g.org + (long long)j * g.sj + k;
+    for (int n0 = 0; n0 < nsteps; n0 += QN) {
+#pragma unroll
+      for (int ph = 0; ph < QN; ++ph) {
+        const int n = n0 + ph;
+        if (n >= nsteps) break;
+        const uint32_t hh = h + (uint32_t)n;
+        const int stage = (int)(hh % NV);
+        if (!mbar_wait_bounded(&full[stage], (hh / NV) & 1u, timeout_ns)) {
+          atomicExch(status, (uint32_t)kDevTimeoutFull);
+          return;
+        }
+        q[ph] = *reinterpret_cast<const float4*>(ur + (hh % NU) * USLOT + (r + R) * UKW +
+                                                 kTmaKHalo + 4 * lane);
+        if (n >= 2 * R) {
+          const int i = ia + n - 2 * R;
+          const float* uc = ur + ((hh - R) % NU) * USLOT + (r + R) * UKW;
+          const float4 c4 = q[(ph + QN - R) % QN];
+          const float4 l4 = *reinterpret_cast<const float4*>(uc + 4 * lane);
+          const float4 r4 = *reinterpret_cast<const float4*>(uc + 2 * kTmaKHalo + 4 * lane);
+          const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w,
+                               r4.x, r4.y, r4.z, r4.w};
+          float acc[4];
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const int ax = pair_axis(P, p);
+            const int rr = pair_r(P, p);
+            float a[4], b[4];
+            if (ax == 2) {
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                a[c] = w[4 + c - rr];
+                b[c] = w[4 + c + rr];
+              }
+            } else if (ax == 1) {
+              const float4 A = *reinterpret_cast<const float4*>(uc - rr * UKW + kTmaKHalo + 4 * lane);
+              const float4 B = *reinterpret_cast<const float4*>(uc + rr * UKW + kTmaKHalo + 4 * lane);
+              a[0] = A.x; a[1] = A.y; a[2] = A.z; a[3] = A.w;
+              b[0] = B.x; b[1] = B.y; b[2] = B.z; b[3] = B.w;
+            } else {
+              const float4 A = q[(ph + 2 * QN - R - rr) % QN];
+              const float4 B = q[(ph + QN - R + rr) % QN];
+              a[0] = A.x; a[1] = A.y; a[2] = A.z; a[3] = A.w;
+              b[0] = B.x; b[1] = B.y; b[2] = B.z; b[3] = B.w;
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const float pr = a[c] + b[c];
+              if (MODE == ST3D_MODE_REF) {
+                acc[c] = __fmaf_rn(cf.cf[p], pr, p == 0 ? cf.coef0 * w[4 + c] : acc[c]);
+              } else {
+                acc[c] = p == 0 ? cf.cf[0] * pr : __fmaf_rn(cf.cf[p], pr, acc[c]);
+              }
+            }
+          }
+          const float4 v4 = *reinterpret_cast<const float4*>(vr + stage * VSLOT + r * TK + 4 * lane);
+          const float4 s4 = *reinterpret_cast<const float4*>(sr + stage * VSLOT + r * TK + 4 * lane);
+          const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+          float ss[4] = {s4.x, s4.y, s4.z, s4.w};
+          float o[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (MODE == ST3D_MODE_REF) {
+              o[c] = __fmaf_rn(ss[c], acc[c], __fmaf_rn(-cf.K, w[4 + c], vv[c]));
+            } else {
+              if (i == src.i && j == src.j && k + c == src.k) ss[c] = ss[c] + src.amp;
+              float t = __fmaf_rn(cf.c0, w[4 + c], -vv[c]);
+              t = __fmaf_rn(cf.c1, acc[c], t);
+              o[c] = __fmaf_rn(cf.c2, ss[c], t);
+            }
+          }
+          if (row_ok) {
+            float* dst = vrow + (long long)i * g.si;
+            if (k + 3 < g.zs) {
+              *reinterpret_cast<float4*>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+            } else {
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                if (k + c < g.zs) dst[c] = o[c];
+            }
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[stage]);
+      }
+    }
+    h += (uint32_t)nsteps;
+  }
+}
+
+template <int P, int MODE, int TJ, int NV>
+cudaError_t launch_cfg(const TmaPlan& plan, const Geom& g, const Coefs<float>& cf, float* v,
+                       int ubuf, int vbuf, int sbuf, const Source& src, uint32_t* dev_status,
+                       cudaStream_t stream) {
+  auto kern = k_tma<P, MODE, TJ, NV>;
+  cudaError_t e =
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
+  if (e != cudaSuccess) return e;
+  kern<<<plan.grid, (TJ + 1) * 32, plan.smem, stream>>>(
+      plan.umap[ubuf], plan.vmap[vbuf], plan.vmap[sbuf], g, cf, v, plan.ntk, plan.ntj * plan.ntk,
+      plan.ichunk, plan.units, src, plan.timeout_ns, dev_status);
+  return cudaGetLastError();
+}
+
+template <int P, int MODE>
+cudaError_t launch_mode(const TmaPlan& plan, const Geom& g, const Coefs<float>& cf, float* v,
+                        int ubuf, int vbuf, int sbuf, const Source& src, uint32_t* dev_status,
+                        cudaStream_t stream) {
+  if (plan.tj == 16 && plan.nv == 3)
+    return launch_cfg<P, MODE, 16, 3>(plan, g, cf, v, ubuf, vbuf, sbuf, src, dev_status, stream);
+  if (plan.tj == 8 && plan.nv == 3)
+    return launch_cfg<P, MODE, 8, 3>(plan, g, cf, v, ubuf, vbuf, sbuf, src, dev_status, stream);
+  if (plan.tj == 8 && plan.nv == 4)
+    return launch_cfg<P, MODE, 8, 4>(plan, g, cf, v, ubuf, vbuf, sbuf, src, dev_status, stream);
+  if (plan.tj == 16 && plan.nv == 2)
+    return launch_cfg<P, MODE, 16, 2>(plan, g, cf, v, ubuf, vbuf, sbuf, src, dev_status, stream);
+  return cudaErrorInvalidConfiguration;
+}
+
+template <int P, int MODE>
+int occupancy_mode(int tj, int nv, size_t smem) {
+  int n = 0;
+  auto probe = [&](auto kern, int threads) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return 0;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, threads, smem) != cudaSuccess)
+      return 0;
+    return b;
+  };
+  if (tj == 16 && nv == 3) n = probe(k_tma<P, MODE, 16, 3>, 17 * 32);
+  if (tj == 8 && nv == 3) n = probe(k_tma<P, MODE, 8, 3>, 9 * 32);
+  if (tj == 8 && nv == 4) n = probe(k_tma<P, MODE, 8, 4>, 9 * 32);
+  if (tj == 16 && nv == 2) n = probe(k_tma<P, MODE, 16, 2>, 17 * 32);
+  cudaGetLastError();
+  return n;
+}
+
+}  // namespace
+
+int tma_blocks_per_sm(int points, int mode, int tj, int nv, size_t smem) {
+  const bool ref = mode == ST3D_MODE_REF;
+  switch (points) {
+    case 7: return ref ? occupancy_mode<7, ST3D_MODE_REF>(tj, nv, smem) : occupancy_mode<7, ST3D_MODE_WAVE>(tj, nv, smem);
+    case 13: return ref ? occupancy_mode<13, ST3D_MODE_REF>(tj, nv, smem) : occupancy_mode<13, ST3D_MODE_WAVE>(tj, nv, smem);
+    case 25: return ref ? occupancy_mode<25, ST3D_MODE_REF>(tj, nv, smem) : occupancy_mode<25, ST3D_MODE_WAVE>(tj, nv, smem);
+    default: return 0;
+  }
+}
+
+bool tma_config_supported(int tj, int nv) {
+  return (tj == 16 && nv == 3) || (tj == 8 && nv == 3) || (tj == 8 && nv == 4) ||
+         (tj == 16 && nv == 2);
+}
+
+cudaError_t launch_tma(const TmaPlan& plan, int points, int mode, const Geom& g,
+                       const Coefs<float>& cf, float* v, int ubuf, int vbuf, int sbuf,
+                       const Source& src, uint32_t* dev_status, cudaStream_t stream) {
+#define ST3D_TMA_CASE(PTS)                                                                  \
+  case PTS:                                                                                 \
+    return mode == ST3D_MODE_REF                                                            \
+               ? launch_mode<PTS, ST3D_MODE_REF>(plan, g, cf, v, ubuf, vbuf, sbuf, src,     \
+                                                 dev_status, stream)                        \
+               : launch_mode<PTS, ST3D_MODE_WAVE>(plan, g, cf, v, ubuf, vbuf, sbuf, src,    \
+                                                  dev_status, stream);
+  switch (points) {
+    ST3D_TMA_CASE(7)
+    ST3D_TMA_CASE(13)
+    ST3D_TMA_CASE(25)
+    default:
+      return cudaErrorInvalidValue;
+  }
+#undef ST3D_TMA_CASE
+}
+
+}  // namespace st3d

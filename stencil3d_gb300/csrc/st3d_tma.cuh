@@ -1,0 +1,136 @@
+// st3d_tma.cuh -- TMA and mbarrier primitives (inline PTX, sm_90+ forms that
+// sm_103a runs) and the TMA-kernel plan shared by the launcher and the
+// context code.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace st3d {
+
+// CTA tile of the TMA kernel: TK = 128 points along k (32 lanes x float4),
+// TJ rows along j (one consumer warp per row), plus a producer warp.
+constexpr int kTmaTK = 128;
+constexpr int kTmaKHalo = 4;                    // floats loaded either side along k (16 bytes)
+constexpr int kTmaUKW = kTmaTK + 2 * kTmaKHalo; // smem row width of a u tile
+
+struct TmaPlan {
+  int tj = 16;      // rows per tile (consumer warps)
+  int nv = 3;       // pipeline stages (v/s ring depth); u ring has nv + R slots
+  int ichunk = 128; // planes per work unit
+  int radius = 0;
+  int ntj = 0, ntk = 0, nti = 0, units = 0;
+  int grid = 0, threads = 0;
+  size_t smem = 0;
+  uint64_t timeout_ns = 4000000000ull;
+  CUtensorMap umap[3];  // halo box (kTmaUKW x (tj+2R) x 1) over each field buffer
+  CUtensorMap vmap[3];  // interior box (kTmaTK x tj x 1) over each field buffer
+};
+
+// Planes per work unit: the chunk length that minimises the modelled time
+// ceil(units / ctas) * (ichunk + R/2) (a unit's 2R warm-up steps load only u,
+// about a quarter of a full step's bytes), i.e. balance across the persistent
+// CTAs against the warm-up re-reads of short chunks.
+inline int tma_pick_ichunk(int xs, int tiles, int ctas, int R) {
+  int best = xs;
+  double best_cost = 1e300;
+  for (int ic = 8; ic <= xs + 7; ++ic) {
+    const int nti = (xs + ic - 1) / ic;
+    const int chunk = (xs + nti - 1) / nti;
+    const long long units = (long long)nti * tiles;
+    const long long waves = (units + ctas - 1) / ctas;
+    const double cost = (double)waves * (chunk + 0.5 * R);
+    if (cost < best_cost - 1e-9) {
+      best_cost = cost;
+      best = chunk;
+    }
+    if (chunk >= xs) break;
+  }
+  return best;
+}
+
+inline size_t tma_smem_bytes(int tj, int nv, int R) {
+  const size_t uslot = ((size_t)kTmaUKW * (tj + 2 * R) + 31) / 32 * 32 * 4;
+  const size_t vslot = (size_t)kTmaTK * tj * 4;
+  return (size_t)(nv + R) * uslot + 2 * (size_t)nv * vslot + 2 * (size_t)nv * 8 + 128;
+}
+
+#ifdef __CUDACC__
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the phase of parity `parity` to complete; gives up after
+// `limit_ns` nanoseconds of wall time (or 2^30 polls) and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint64_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 1; it < (1u << 30); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 31u) == 0 && global_ns() - t0 > limit_ns) return false;
+  }
+  return false;
+}
+
+// 3-D tiled TMA load of the box at element coordinates (x, y, z) into
+// shared memory, completing on `bar` with the box's byte count.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+#endif  // __CUDACC__
+
+}  // namespace st3d

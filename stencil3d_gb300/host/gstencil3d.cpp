@@ -1,0 +1,164 @@
+// gstencil3d -- the hstencil3d command line on one GB300.
+//
+// Same flags, limits, phase log, known-answer checks and report line as the
+// reference driver (main.cpp:94-332): the time loop runs on the GPU through
+// the C ABI, every other step stays on the host.  The stencil size, CPU
+// traversal (PAR2D/HILBERT/...) and `real` are compile-time choices in the
+// reference (config.h:19-65); here the stencil is a run-time flag and the
+// traversal flags are accepted and ignored.
+//
+// Added flags: --stencil N (2, 7, 13, 25; default 7 as config.h:38),
+// --wave (the leapfrog form, README.md:11-20, with --vel/--dt/--dx),
+// --kernel simple|tma|auto.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "st3d_compat.hpp"
+
+namespace {
+
+constexpr unsigned kDefaultHaloXY = 4;    // config.h:4
+constexpr unsigned kDefaultHaloZ = 16;    // config.h:5
+constexpr unsigned kDefaultSizeXY = 945;  // config.h:6
+constexpr unsigned kDefaultSizeZ = 880;   // config.h:7
+constexpr unsigned kDefaultOfs = 16;      // config.h:8
+constexpr unsigned kDefaultIter = 100;    // config.h:9
+
+double flops_per_stencil(int points) {  // config.h:67-91
+  return points == 2 ? 2 : points == 7 ? 12 : points == 13 ? 29 : 41;
+}
+double mem_reals_per_stencil(int points) { return points == 2 ? 2 : 4; }
+double cache_reals_per_stencil(int points) {
+  return points == 2 ? 2 : points == 7 ? 10 : points == 13 ? 16 : 28;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  unsigned train = 0, wave = 0;
+  unsigned offset = kDefaultOfs;
+  unsigned maxiter = kDefaultIter;
+  unsigned cacheiter = 1, dups = 1, prefetch = 64;
+  unsigned xs = kDefaultSizeXY, ys = kDefaultSizeXY, zs = kDefaultSizeZ;
+  unsigned xh = kDefaultHaloXY, yh = kDefaultHaloXY, zh = kDefaultHaloZ;
+  unsigned xb = 1, yb = 1, zb = 16;
+  unsigned jshuffle = 13, kshuffle = 3;
+  unsigned points = 7;
+  real sbm = 12;
+  const char* kernel = "auto";
+  gb300_options gopt;
+
+  int iarg = 1;
+  while (iarg < argc) {
+    int args = 0;
+    args += get_int_arg(argv, iarg, argc, "--iter", maxiter, 1, 100000, 1);
+    args += get_int_arg(argv, iarg, argc, "--citer", cacheiter, 1, 100000, 1);
+    args += get_int_arg(argv, iarg, argc, "--dups", dups, 1, 64, 1);
+    args += get_int_arg(argv, iarg, argc, "--ofs", offset, 0, 16384, 1);
+    args += get_int_arg(argv, iarg, argc, "--pref", prefetch, 1, 512, 1);
+    args += get_int_arg(argv, iarg, argc, "--xh", xh, 4, 16, 1);
+    args += get_int_arg(argv, iarg, argc, "--yh", yh, 4, 16, 1);
+    args += get_int_arg(argv, iarg, argc, "--zh", zh, 1, 16, 1);
+    args += get_int_arg(argv, iarg, argc, "--xs", xs, 1, 1264, 1);
+    args += get_int_arg(argv, iarg, argc, "--ys", ys, 1, 1264, 1);
+    args += get_int_arg(argv, iarg, argc, "--zs", zs, 1, 1264, 1);
+    args += get_int_arg(argv, iarg, argc, "--xb", xb, 1, 1264, 1);
+    args += get_int_arg(argv, iarg, argc, "--yb", yb, 1, 1264, 1);
+    args += get_int_arg(argv, iarg, argc, "--zb", zb, 1, 1264, 1);
+    args += get_real_arg(argv, iarg, argc, "--sbm", sbm, 1.0, 10.0);
+    args += get_flag(argv, iarg, argc, "--train", train);
+    args += get_int_arg(argv, iarg, argc, "--stencil", points, 2, 25, 1);
+    args += get_flag(argv, iarg, argc, "--wave", wave);
+    args += get_double_arg(argv, iarg, argc, "--vel", gopt.vel, 1.0, 1e5);
+    args += get_double_arg(argv, iarg, argc, "--dt", gopt.dt, 1e-9, 1.0);
+    args += get_double_arg(argv, iarg, argc, "--dx", gopt.dx, 1e-6, 1e6);
+    args += get_str_arg(argv, iarg, argc, "--kernel", kernel);
+    if (args > 0) {
+      iarg += args;
+    } else {
+      fprintf(stderr, "unsupported argument %s\n", argv[iarg]);
+      return 2;
+    }
+  }
+  if (points != 2 && points != 7 && points != 13 && points != 25) {
+    fprintf(stderr, "--stencil must be 2, 7, 13 or 25\n");
+    return 2;
+  }
+  if ((ys % yb) != 0) {  // main.cpp:171-174
+    fprintf(stderr, "ERROR: --ys must by an exact multiple of --yb\n");
+    exit(2);
+  }
+  const unsigned radius = points == 25 ? 4 : points == 13 ? 2 : 1;
+  if (zh < radius) {
+    fprintf(stderr, "--zh must be larger or equal to %u for the %u-point stencil\n", radius, points);
+    exit(2);
+  }
+  gopt.points = (int)points;
+  gopt.mode = wave ? ST3D_MODE_WAVE : ST3D_MODE_REF;
+  gopt.kernel = strcmp(kernel, "simple") == 0 ? ST3D_KERNEL_SIMPLE
+              : strcmp(kernel, "tma") == 0    ? ST3D_KERNEL_TMA
+                                              : ST3D_KERNEL_AUTO;
+  gb300_configure(gopt);
+
+  s_grid grid(xs, ys, zs, xh, yh, zh, xb, yb, zb, sbm, jshuffle, kshuffle);
+  const double flops = flops_per_stencil(points) * 1.0e-9 * (double)grid.gvol * maxiter * cacheiter;
+  const double mem_bytes =
+      mem_reals_per_stencil(points) * sizeof(real) * 1.0e-9 * (double)grid.gvol * maxiter * cacheiter;
+  const double cache_bytes =
+      cache_reals_per_stencil(points) * sizeof(real) * 1.0e-9 * (double)grid.gvol * maxiter * cacheiter;
+  const int my_rank = 0;
+  int phase = 0;
+
+  printf("running STENCIL(%d) benchmark: \n", points);
+  printf(" -- using a grid size of %dx%dx%d with a halo of %dx%dx%d elements totaling %f GB\n",
+         grid.xsize, grid.ysize, grid.zsize, grid.xhalo, grid.yhalo, grid.zhalo,
+         1e-9 * (double)grid.gsize * sizeof(real));
+  printf(" -- using block tile size of %d x %d x %d\n", grid.xb_size, grid.yb_size, grid.zb_size);
+  printf(" -- GB300: %s form, %s kernel, one GPU\n", wave ? "leapfrog wave" : "reference",
+         kernel);
+
+  // pinned host arrays, shifted like main.cpp:272-275
+  const size_t page = 1UL << 16;
+  const size_t asize = (((grid.gsize + 64 * (size_t)offset) * sizeof(real) / page) + 1) * page;
+  real *ov = nullptr, *os = nullptr, *ou = nullptr;
+  if (st3d_host_alloc(asize, (void**)&ov) || st3d_host_alloc(asize, (void**)&os) ||
+      st3d_host_alloc(asize, (void**)&ou)) {
+    fprintf(stderr, "error allocating host arrays: %s\n", st3d_last_error());
+    exit(3);
+  }
+  real* v = ov;
+  real* s = os + (size_t)offset * 13;
+  real* u = ou + (size_t)offset * 42;
+
+  printf("[rank%i] Phase #%i: array initialization\n", my_rank, ++phase);
+  double t0 = seconds();
+  init_arrays(ov, os, ou, asize / sizeof(real));
+  double t1 = seconds();
+  printf("[rank%i] Phase #%i: initialization took %f secs\n", my_rank, ++phase, t1 - t0);
+
+  printf("[rank%i] Phase #%i: initial warmup\n", my_rank, ++phase);
+  t0 = seconds();
+  iterate_gb300(v, s, u, grid, prefetch, dups, 1U, cacheiter);
+  t1 = seconds();
+  printf("[rank%i] Phase #%i: finish warmup in %f secs\n", my_rank, ++phase, t1 - t0);
+  if (!wave) check(v, grid, 1U);
+
+  printf("[rank%i] Phase #%i: start compute\n", my_rank, ++phase);
+  iterate_gb300(v, s, u, grid, prefetch, dups, maxiter, cacheiter);
+  const gb300_timing& tm = gb300_last_timing();
+  const double tc = tm.device_ms * 1e-3;  // compute only, as main.cpp:306-308 times ITERATE
+  printf("[rank%i] Phase #%i: finish compute in %f secs (%f GFlop/s, mem: %f GB/s, cache: %f GB/s)\n",
+         my_rank, ++phase, tc, flops / tc, mem_bytes / tc / cacheiter, cache_bytes / tc);
+  printf("gb300: %.3f Gpts/s on the device, %.3f Gpts/s end to end (%.3f s incl. host<->device copies)\n",
+         1e-9 * (double)grid.gvol * maxiter / tc, 1e-9 * (double)grid.gvol * maxiter / tm.total_s,
+         tm.total_s);
+  if (!wave) check(v, grid, maxiter + 1);
+  printf("freeing data arrays\n");
+  gb300_release();
+  st3d_host_free(ov);
+  st3d_host_free(os);
+  st3d_host_free(ou);
+  printf("[rank%i] Phase #%i: done!\n", my_rank, ++phase);
+  return 0;
+}

@@ -1,0 +1,185 @@
+"""The oracle (oracle/st3d_oracle.c) against the reference.
+
+Pins the C restatement to the reference's own host path: against the golden
+fixtures generated from the compiled reference (tests/golden/), against the
+live reference where it was built on this machine (oracle/_ref), and against
+the reference's only built-in test, the constant-field known-answer check of
+iterators.cpp:292-325.
+"""
+import hashlib
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import build as obuild
+from oracle import oracle as O
+from tests.helpers import golden_cases, mode_r_inputs, np_dtype, wave_inputs, rel_l2
+
+META, ARRAYS = golden_cases()
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("case", META, ids=[m["name"] for m in META])
+def test_oracle_matches_reference_golden(case):
+    """Plain flavour of the oracle == the reference, bit for bit."""
+    grid = tuple(case["grid"])
+    v, s, u = mode_r_inputs(grid, case["seed"], case["dtype"])
+    O.iterate_ref(v, s, u, grid, case["points"], case["iterations"])
+    inner = np.ascontiguousarray(O.interior(v, grid))
+    assert _digest(inner) == case["sha256"]
+    if case["keep"]:
+        np.testing.assert_array_equal(inner, ARRAYS[case["name"]])
+
+
+@pytest.mark.parametrize("case", META, ids=[m["name"] for m in META])
+def test_fma_flavour_within_tolerance(case):
+    """The fused flavour (the device kernels' operation order) stays within
+    the 1e-5 relative-L2 parity bound of the reference result."""
+    grid = tuple(case["grid"])
+    v, s, u = mode_r_inputs(grid, case["seed"], case["dtype"])
+    O.iterate_ref(v, s, u, grid, case["points"], case["iterations"], fma=True)
+    inner = O.interior(v, grid)
+    ref = ARRAYS.get(case["name"])
+    if ref is None:
+        v2, s2, u2 = mode_r_inputs(grid, case["seed"], case["dtype"])
+        O.iterate_ref(v2, s2, u2, grid, case["points"], case["iterations"])
+        ref = O.interior(v2, grid)
+    tol = 1e-14 if case["dtype"] == "f64" else 1e-6
+    assert rel_l2(inner, ref) <= tol
+
+
+@pytest.mark.parametrize("points", [7, 13, 25])
+def test_known_answer(points):
+    """init_arrays + check (iterators.cpp:292-325): after n steps v == n."""
+    grid = (16, 12, 20, 4, 4, 16)
+    v, s, u = O.init_arrays(grid)
+    O.iterate_ref(v, s, u, grid, points, 1)
+    assert O.check(v, grid, 1) == 0
+    O.iterate_ref(v, s, u, grid, points, 6)
+    assert O.check(v, grid, 7) == 0
+    if points == 7:  # coefficients sum exactly to 1 in float only for 7 points
+        assert np.all(O.interior(v, grid) == 7.0)
+
+
+def test_two_point_fails_known_answer_like_reference():
+    """stencil_2 has no v accumulation (stencil_2.h:27), so the reference's own
+    check reports every point; the oracle reproduces that."""
+    grid = (6, 5, 8, 4, 4, 1)
+    v, s, u = O.init_arrays(grid)
+    O.iterate_ref(v, s, u, grid, 2, 3)
+    assert O.check(v, grid, 3) == 6 * 5 * 8
+
+
+def test_halos_never_written():
+    grid = (7, 6, 9, 4, 4, 4)
+    v, s, u = mode_r_inputs(grid, 3, "f32")
+    v0 = v.copy()
+    O.iterate_ref(v, s, u, grid, 25, 2)
+    mask = np.ones(v.shape, bool)
+    mask[4:11, 4:10, 4:13] = False
+    np.testing.assert_array_equal(v[mask], v0[mask])
+
+
+def test_default_coefficients_match_reference_constants():
+    c = O.default_coefs(25, np.float32)
+    assert c[0] == np.float32(1.25) and c[1] == np.float32(6.25)
+    assert c[6] == np.float32(np.float32(0.4) * np.float32(1.1))
+    d = O.default_coefs(25, np.float64)
+    assert d[6] == float(np.float32(0.4)) * float(np.float32(1.1))
+    c13 = O.default_coefs(13, np.float32)
+    assert c13[1] == np.float32(3.5) and c13[10] == np.float32(np.float32(0.3) * np.float32(0.9))
+
+
+ref_built = pytest.mark.skipif(not O.ref_available(7), reason="reference not built on this machine")
+
+
+@ref_built
+@pytest.mark.parametrize("points", [2, 7, 13, 25])
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_oracle_matches_live_reference(points, dtype):
+    grid = (9, 14, 27, 4, 5, 7)
+    v1, s, u = mode_r_inputs(grid, 101 + points, dtype)
+    v2 = v1.copy()
+    O.iterate_ref(v1, s, u, grid, points, 4)
+    O.ref_iterate(v2, s, u, grid, points, 4)
+    np.testing.assert_array_equal(v1, v2)
+
+
+@ref_built
+def test_oracle_matches_reference_iterate_3d_square():
+    """iterate_3d (the README host recipe) agrees on square grids; it bounds j by
+    isize (iterators.cpp:146) so non-square grids are not comparable."""
+    grid = (12, 12, 20, 4, 4, 16)
+    v1, s, u = mode_r_inputs(grid, 5, "f32")
+    v2 = v1.copy()
+    O.iterate_ref(v1, s, u, grid, 13, 3)
+    O.ref_iterate(v2, s, u, grid, 13, 3, traversal="3d")
+    np.testing.assert_array_equal(v1, v2)
+
+
+@ref_built
+@pytest.mark.parametrize("points", [7, 13, 25])
+def test_reference_binary_known_answer(points):
+    exe = os.path.join(obuild.REF_DIR, "hstencil3d_%d" % points)
+    r = subprocess.run([exe, "--xs", "24", "--ys", "24", "--zs", "32", "--iter", "3"],
+                       capture_output=True, text=True, env=dict(os.environ, OMP_NUM_THREADS="2"),
+                       timeout=60)
+    assert r.returncode == 0
+    assert r.stdout.count("check: 0 errors found") == 2
+
+
+# ---------------------------------------------------------------- mode W ---
+def test_wave_oracle_fp32_tracks_fp64():
+    grid = (24, 20, 28, 4, 4, 4)
+    c0, c1, c2 = O.wave_constants(13, 1500.0, 5e-4, 10.0)
+    v, s, u = wave_inputs(grid, 9)
+    vd, sd, ud = v.astype(np.float64), s.astype(np.float64), u.astype(np.float64)
+    amps = O.ricker_amps(0, 30, 5e-4)
+    src = (12, 10, 14)
+    O.iterate_wave(u, v, s, grid, 13, 30, c0, c1, c2, src=src, amps=amps)
+    O.iterate_wave(ud, vd, sd, grid, 13, 30, c0, c1, c2, src=src,
+                   amps=O.ricker_amps(0, 30, 5e-4, dtype=np.float64))
+    assert rel_l2(O.interior(u, grid), O.interior(ud, grid)) < 1e-5
+
+
+def test_wave_oracle_fma_and_plain_agree():
+    grid = (16, 18, 20, 4, 4, 4)
+    c0, c1, c2 = O.wave_constants(25, 1500.0, 5e-4, 10.0)
+    v, s, u = wave_inputs(grid, 4)
+    v2, s2, u2 = v.copy(), s.copy(), u.copy()
+    O.iterate_wave(u, v, s, grid, 25, 10, c0, c1, c2, fma=True)
+    O.iterate_wave(u2, v2, s2, grid, 25, 10, c0, c1, c2, fma=False)
+    assert rel_l2(O.interior(u, grid), O.interior(u2, grid)) < 1e-6
+
+
+def test_wave_constant_field_is_stationary():
+    """c0 = 2 - 2*c1*sum(w) makes u = v = const a fixed point (up to rounding)."""
+    grid = (10, 10, 10, 4, 4, 4)
+    for pts in (7, 13, 25):
+        c0, c1, c2 = O.wave_constants(pts, 1500.0, 1e-3 if pts == 7 else 5e-4, 10.0)
+        u = np.full(O.shape(grid), 0.5, np.float64)
+        v = u.copy()
+        s = np.zeros_like(u)
+        O.iterate_wave(u, v, s, grid, pts, 5, c0, c1, c2)
+        assert np.max(np.abs(O.interior(u, grid) - 0.5)) < 1e-12
+
+
+def test_wave_ricker_source():
+    t0 = 1.0 / 15.0
+    assert O.ricker(t0) == 1.0
+    assert abs(O.ricker(0.0)) < 1e-3
+    a = O.ricker_amps(0, 200, 1e-3)
+    assert np.argmax(a) == 67  # t = 0.067 s, the sample nearest t0
+
+
+def test_wave_weights_follow_readme_for_seven_points():
+    w = O.wave_weights(7)
+    assert w[2] == w[6] == w[10] == 1.0
+    c0, c1, c2 = O.wave_constants(7, 1500.0, 1e-3, 10.0)
+    assert abs(c1 - 0.0225) < 1e-15 and abs(c2 - 1e-6) < 1e-18
+    assert abs(c0 - (2 - 6 * 0.0225)) < 1e-15
