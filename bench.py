@@ -40,6 +40,7 @@ sys.path.insert(0, REPO)
 WORKLOADS = {
     # name: (points, xs, ys, zs, halo, dt, init)
     "wave25_1024": (25, 1024, 1024, 1024, 4, 5e-4, "blobs"),
+    "wave25_512": (25, 512, 512, 512, 4, 5e-4, "blobs"),
     "wave25_528": (25, 528, 528, 528, 4, 5e-4, "uniform"),
     "wave13_1040": (13, 1040, 1040, 1040, 2, 5e-4, "blobs"),
     "wave7_256": (7, 256, 256, 256, 1, 1e-3, "uniform"),

@@ -54,7 +54,10 @@ typedef enum st3d_mode {
   ST3D_MODE_REF = 0,
   /* Leapfrog acoustic wave (README.md:11-20):
    *   v <- c0*u - v + c1*sum w_{axis,r}*(u[-r] + u[+r]) + c2*(s + a_n*delta_src)
-   * then u and v swap roles.  a_n is a Ricker wavelet at step n. */
+   * then u and v swap roles.  a_n is a Ricker wavelet at step n.  With
+   * c0 = 2 - 2*c1*sum(w) it is evaluated as (2u - v) + c1*sum w*((u[-r] +
+   * u[+r]) - 2u) + c2*s, which keeps constant fields exact in any precision
+   * (the literal form lets FP32 drift ~5e-3 from FP64 in 1000 steps). */
   ST3D_MODE_WAVE = 1
 } st3d_mode;
 
@@ -135,8 +138,8 @@ const char* st3d_last_error(void);
 /* Current device: SM count, compute capability, total memory. */
 int st3d_device_info(int* sm_count, int* cc_major, int* cc_minor, size_t* total_bytes);
 
-/* Defaults: the reference's CONSTANTS_* for `points` (stencil_*.h; for F64
- * storage the double products of config.h's real=double build), mode W
+/* Defaults: the reference's CONSTANTS_* for `points` (stencil_*.h; for mode R
+ * with F64 storage the double products of config.h's real=double build), mode W
  * weights 1 for 7 points (README.md:11-20) and stencil_*.h cx/cy/cz for 13 and
  * 25, c = 1500 m/s, dx = 10 m, dt = 1 ms, 15 Hz Ricker with t0 = 1/f at the
  * grid centre (set at st3d_create when src_i = -2). */

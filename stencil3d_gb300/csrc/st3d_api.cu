@@ -329,7 +329,10 @@ int st3d_default_opts(int points, int mode, int storage, st3d_opts* o) {
   o->src_i = -2;  // grid centre, resolved at st3d_create
   o->src_f = 15.0;
   o->src_t0 = 1.0 / 15.0;
-  const bool dbl = storage == ST3D_F64;
+  // Mode W has no reference code; its weights are the float constants of
+  // stencil_*.h for every storage, so an FP64 run is the same stencil as the
+  // FP32 run it judges.
+  const bool dbl = storage == ST3D_F64 && mode == ST3D_MODE_REF;
   // The reference's CONSTANTS_* (stencil_7.h:4-8, stencil_13.h:4-22,
   // stencil_25.h:20-34).  The y/z coefficients are products formed in the
   // type of `real` (config.h:96-100): float products widened for float

@@ -12,9 +12,13 @@
 //   mode R (stencil_7.h:31-39, stencil_13.h:50-61, stencil_25.h:75-95):
 //     st = coef0*u0; st = fma(cf_p, u[-r]+u[+r], st) ...;
 //     v = fma(s0, st, fma(-K, u0, v0))
-//   mode W (README.md:11-20):
-//     lap = cf_0*(u[-r]+u[+r]); lap = fma(cf_p, ..., lap) ...;
-//     v = fma(c2, s_eff, fma(c1, lap, fma(c0, u0, -v0)))
+//   mode W (README.md:11-20, c0 = 2 - 2*c1*sum(w)), difference form, u2 = 2*u0:
+//     lap = cf_0*((u[-r]+u[+r]) - u2); lap = fma(cf_p, (u[-r]+u[+r]) - u2, lap) ...;
+//     v = fma(c2, s_eff, fma(c1, lap, u2 - v0))
+//   Algebraically c0*u - v + c1*sum(w*(u[-r]+u[+r])) + c2*s; the difference
+//   form keeps constant fields exactly constant, where the literal form's
+//   separately rounded c0 lets the smoothest modes drift (about 5e-3 relative
+//   L2 against FP64 after 1000 FP32 steps of a blob field, against 1e-5).
 //   2 points (stencil_2.h:20-29): v = coef0*(u0 + u[k+1])
 // The library is built with -fmad=false, so these are the only fused
 // operations, the sequence oracle/st3d_oracle.c's fma flavour reproduces.
@@ -86,10 +90,11 @@ __global__ void __launch_bounds__(kSimpleBX* kSimpleBY)
       out = fma_t<T>(s0, st, fma_t<T>(-cf.K, u0, v0));
     } else {
       if (i == src_i && j == src_j && k == src_k) s0 = s0 + amp;
-      T lap = cf.cf[0] * pr[0];
+      const T u2 = u0 + u0;
+      T lap = cf.cf[0] * (pr[0] - u2);
 #pragma unroll
-      for (int p = 1; p < NP; ++p) lap = fma_t<T>(cf.cf[p], pr[p], lap);
-      T t = fma_t<T>(cf.c0, u0, -v0);
+      for (int p = 1; p < NP; ++p) lap = fma_t<T>(cf.cf[p], pr[p] - u2, lap);
+      T t = u2 - v0;
       t = fma_t<T>(cf.c1, lap, t);
       out = fma_t<T>(cf.c2, s0, t);
     }

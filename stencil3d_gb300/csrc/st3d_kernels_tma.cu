@@ -197,7 +197,8 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
               if (MODE == ST3D_MODE_REF) {
                 acc[c] = __fmaf_rn(cf.cf[p], pr, p == 0 ? cf.coef0 * w[4 + c] : acc[c]);
               } else {
-                acc[c] = p == 0 ? cf.cf[0] * pr : __fmaf_rn(cf.cf[p], pr, acc[c]);
+                const float d = pr - (w[4 + c] + w[4 + c]);
+                acc[c] = p == 0 ? cf.cf[0] * d : __fmaf_rn(cf.cf[p], d, acc[c]);
               }
             }
           }
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
               o[c] = __fmaf_rn(ss[c], acc[c], __fmaf_rn(-cf.K, w[4 + c], vv[c]));
             } else {
               if (i == src.i && j == src.j && k + c == src.k) ss[c] = ss[c] + src.amp;
-              float t = __fmaf_rn(cf.c0, w[4 + c], -vv[c]);
+              float t = (w[4 + c] + w[4 + c]) - vv[c];
               t = __fmaf_rn(cf.c1, acc[c], t);
               o[c] = __fmaf_rn(cf.c2, ss[c], t);
             }

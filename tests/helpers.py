@@ -30,15 +30,25 @@ def mode_r_inputs(grid, seed, dtype):
     return v, s, u
 
 
+def halo_mask(grid):
+    xs, ys, zs, xh, yh, zh = grid
+    m = np.ones(O.shape(grid), bool)
+    m[xh:xh + xs, yh:yh + ys, zh:zh + zs] = False
+    return m
+
+
 def wave_inputs(grid, seed, dtype=np.float32, blobs=False):
     """Wave-form inputs: u, v ~ U[-1e-3, 1e-3) (or seeded Gaussian blobs with
-    v = u), s = 0."""
+    v = u), s = 0.  The halo is a fixed Dirichlet boundary: u's seeded halo
+    values, the same in v, so that it does not change when u and v swap."""
     if blobs:
         u = O.fill_blobs(grid, seed, 8, 20.0, dtype)
         v = u.copy()
     else:
         u = O.fill_uniform(grid, seed, 0, -1e-3, 1e-3, dtype)
         v = O.fill_uniform(grid, seed, 1, -1e-3, 1e-3, dtype)
+        m = halo_mask(grid)
+        v[m] = u[m]
     s = np.zeros_like(u)
     return v, s, u
 
