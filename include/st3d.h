@@ -192,6 +192,22 @@ int st3d_check(st3d_ctx* ctx, double expected, double tol, uint64_t* errors);
  * out[0] = sum (a-b)^2, out[1] = sum b^2, out[2] = max|a-b|, out[3] = max|b|. */
 int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]);
 
+/* FP64 norms without any allocation.  No counterpart in the reference.
+ * For callers that cannot allocate device memory when they check drift, such
+ * as a solver running inside another application's time loop on buffers that
+ * application owns, where cudaMalloc/cudaFree may synchronise the device or
+ * fail because the memory is reserved.  a and b (b may be NULL) are device
+ * fields in the reference layout of `grid` (float for ST3D_F32, double for
+ * ST3D_F64); out_dev is device memory for 4 doubles with the meaning of
+ * st3d_norms' out; the work is enqueued on `stream` (a cudaStream_t, NULL for
+ * the legacy default stream) and nothing is synchronised.  Partial sums live
+ * in a 128 KiB array inside the library image: at most 4096 planes along i
+ * (larger grids are rejected with ST3D_ERR_INVALID), calls that overlap on
+ * the GPU race on it and must be serialised, and the first call on a device
+ * looks up the array's address, so make it before any stream capture. */
+int st3d_norms_noalloc(const st3d_grid_desc* grid, const void* a, int storage_a, const void* b,
+                       int storage_b, double* out_dev, void* stream);
+
 /* CUDA-event timing on the context's stream. */
 int st3d_timer_start(st3d_ctx* ctx);
 int st3d_timer_stop(st3d_ctx* ctx, float* ms);

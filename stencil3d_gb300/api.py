@@ -99,6 +99,7 @@ def lib():
             "st3d_host_alloc": ([C.c_size_t, C.POINTER(vp)], i),
             "st3d_host_free": ([vp], i),
             "st3d_ricker": ([C.c_double, C.c_double, C.c_double], C.c_double),
+            "st3d_norms_noalloc": ([C.POINTER(GridDesc), vp, i, vp, i, vp, vp], i),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

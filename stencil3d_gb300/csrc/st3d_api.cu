@@ -67,6 +67,16 @@ int host_elem_bytes(int storage) { return storage == ST3D_F64 ? 8 : 4; }
 
 namespace st3d {
 
+int set_error(int status, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return status;
+}
+
 Layout make_layout(uint32_t xs, uint32_t ys, uint32_t zs, int eb) {
   Layout L;
   L.xs = xs; L.ys = ys; L.zs = zs;

@@ -100,6 +100,9 @@ enum DeviceStatus : uint32_t {
   kDevTimeoutEmpty = 2,
 };
 
+// Records a formatted message for st3d_last_error() and returns `status`.
+int set_error(int status, const char* fmt, ...);
+
 // ---- kernel launchers (st3d_kernels_*.cu) --------------------------------
 // All launch on `stream` and return the cudaGetLastError() of the launch.
 cudaError_t launch_simple(int points, int mode, int storage, const Geom& g, const void* coefs,
