@@ -236,11 +236,11 @@ def e2e_run(S, st, g, calls, iters):
             p.free()
     pts = g.gvol
     ms = statistics.median(times)
-    # bytes copied per call, counted from the copied regions
+    # bytes copied per call: each upload moves a whole host array, each
+    # download the span of the interior rows of every interior plane
     xs, ys, zs = g.xsize, g.ysize, g.zsize
-    h = min(g.xhalo, 4)
-    h2d = 3 * (xs + 2 * h) * (ys + 2 * h) * (zs + 2 * h) * 4
-    d2h = 2 * xs * ys * zs * 4
+    h2d = 3 * g.gsize * 4
+    d2h = 2 * xs * ys * (zs + 2 * g.zhalo) * 4
     return {"value": pts * iters / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "step": "one ITERATE-equivalent call (st3d_iterate_host) of %d time steps" % iters,

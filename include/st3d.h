@@ -163,13 +163,19 @@ int st3d_get_info(const st3d_ctx* ctx, st3d_info* info);
 /* The context's CUDA stream (a cudaStream_t), for callers that order work. */
 int st3d_get_stream(const st3d_ctx* ctx, void** stream);
 
-/* Copy reference-layout host arrays in (NULL: leave that field).  u and v
- * are copied with min(halo, 4) halo points per side (the stencil reads u's
- * halo), s likewise.  Resets the mode W step clock to 0. */
+/* Copy reference-layout host arrays in (NULL: leave that field): interior,
+ * min(halo, 4) halo planes and rows, and the k halo (the stencil reads u's
+ * halo).  One contiguous host-to-device copy per field through a staging
+ * buffer the context allocates on first use (the size of one host array).
+ * Resets the mode W step clock to 0. */
 int st3d_upload(st3d_ctx* ctx, const void* v, const void* s, const void* u);
-/* Copy interior points out (halos of the host arrays are not written,
- * as the reference never writes halos).  Mode W: u = newest field U^n,
- * v = U^{n-1}.  NULL: skip. */
+/* Copy interior points out: the host arrays' halo planes and rows are not
+ * written, as the reference never writes halos; the k-halo points between
+ * interior rows are rewritten with the device's copy of them (one 2-D copy
+ * per field moves whole plane spans): in mode R the values uploaded for that
+ * same array, in mode W those of the buffer that holds the field, so u and v
+ * should carry the same halo (a fixed boundary).  Mode W: u = newest field
+ * U^n, v = U^{n-1}.  NULL: skip. */
 int st3d_download(st3d_ctx* ctx, void* v, void* u);
 /* Replaces ITERATE(v,s,u,grid,prefetch,dups,iterations,cacheiter)
  * (iterators.h:6-29, iterators.cpp:130-289) on device-resident fields:

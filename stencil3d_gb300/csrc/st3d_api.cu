@@ -134,6 +134,8 @@ struct st3d_ctx {
   bool has_u = false, has_v = false, has_s = false;
   int device = 0;
   TmaPlan* tma = nullptr;
+  void* stage = nullptr;      // reference-layout staging buffer for host copies
+  size_t stage_bytes = 0;
   Coefs<float> cf32;
   Coefs<double> cf64;
   size_t bytes = 0;
@@ -246,9 +248,51 @@ void* v_ptr(st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->fld[1 - c-
 int u_index(const st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->cur : 0; }
 int v_index(const st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? 1 - c->cur : 1; }
 
-// Host (reference layout) <-> device (library layout) copy of one field.
-// `halo` points per side along each axis, capped by the host halos.
-int copy_field(st3d_ctx* c, void* dev, void* host, bool to_device, bool with_halo) {
+RefGeom ref_geom(const st3d_grid_desc& g) {
+  RefGeom R;
+  R.xs = (int)g.xs; R.ys = (int)g.ys; R.zs = (int)g.zs;
+  R.jmult = (long long)g.zs + 2LL * g.zh;
+  R.imult = R.jmult * ((long long)g.ys + 2LL * g.yh);
+  R.ijk_ofs = (long long)g.zh + (long long)g.yh * R.jmult + (long long)g.xh * R.imult;
+  return R;
+}
+
+size_t host_array_bytes(const st3d_ctx* c) {
+  const st3d_grid_desc& g = c->grid;
+  return ((size_t)g.xs + 2 * g.xh) * ((size_t)g.ys + 2 * g.yh) * ((size_t)g.zs + 2 * g.zh) *
+         host_elem_bytes(c->opts.storage);
+}
+
+// The staged path needs the halo along k to fit the device row pad and the
+// launch grid (rows x planes) to fit 65535 x 65535.
+bool staged_ok(const st3d_ctx* c) {
+  const st3d_grid_desc& g = c->grid;
+  return host_elem_bytes(c->opts.storage) == c->eb && g.zh <= c->L.pk &&
+         g.ys + 8 <= 65535 && g.xs + 8 <= 65535;
+}
+
+int ensure_stage(st3d_ctx* c) {
+  const size_t need = host_array_bytes(c);
+  if (c->stage && c->stage_bytes >= need) return ST3D_OK;
+  if (c->stage) {
+    cudaFree(c->stage);
+    c->bytes -= c->stage_bytes;
+    c->stage = nullptr;
+  }
+  cudaError_t e = cudaMalloc(&c->stage, need);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    c->stage = nullptr;
+    return fail(ST3D_ERR_NOMEM, "cudaMalloc of the %zu-byte staging buffer failed", need);
+  }
+  c->stage_bytes = need;
+  c->bytes += need;
+  return ST3D_OK;
+}
+
+// Strided host<->device copy of one field (fallback when the staged path does
+// not apply): interior plus min(halo, 4) per side when `with_halo`.
+int copy_field_strided(st3d_ctx* c, void* dev, void* host, bool to_device, bool with_halo) {
   const st3d_grid_desc& g = c->grid;
   const int hb = host_elem_bytes(c->opts.storage);
   const uint32_t hx = with_halo ? (g.xh < 4 ? g.xh : 4) : 0;
@@ -270,6 +314,40 @@ int copy_field(st3d_ctx* c, void* dev, void* host, bool to_device, bool with_hal
   }
   p.extent = make_cudaExtent((g.zs + 2 * hz) * (size_t)hb, g.ys + 2 * hy, g.xs + 2 * hx);
   ST3D_CUDA(cudaMemcpy3DAsync(&p, c->stream));
+  return ST3D_OK;
+}
+
+// Host (reference layout) -> device field: one contiguous copy into the
+// staging buffer, then a scatter kernel into the library layout (interior,
+// min(halo, 4) planes and rows, all k-halo points up to the row pad).
+int upload_field(st3d_ctx* c, void* dev, const void* host) {
+  if (!staged_ok(c)) return copy_field_strided(c, dev, const_cast<void*>(host), true, true);
+  int rc = ensure_stage(c);
+  if (rc != ST3D_OK) return rc;
+  ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyHostToDevice, c->stream));
+  const st3d_grid_desc& g = c->grid;
+  const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4;
+  cudaError_t e = launch_ref_to_dev(c->eb, c->L, ref_geom(g), c->stage, dev, hx, hy, (int)g.zh, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "upload scatter kernel");
+  return ST3D_OK;
+}
+
+// Device field -> host (reference layout), interior points only: a gather
+// kernel writes every interior row with its k halo into the staging buffer,
+// then one 2-D copy moves per i-plane the span of the ys interior rows.
+int download_field(st3d_ctx* c, const void* dev, void* host) {
+  if (!staged_ok(c)) return copy_field_strided(c, const_cast<void*>(dev), host, false, false);
+  int rc = ensure_stage(c);
+  if (rc != ST3D_OK) return rc;
+  const st3d_grid_desc& g = c->grid;
+  const RefGeom R = ref_geom(g);
+  cudaError_t e = launch_dev_to_ref(c->eb, c->L, R, dev, c->stage, (int)g.zh, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "download gather kernel");
+  const size_t hb = host_elem_bytes(c->opts.storage);
+  const size_t off = ((size_t)g.xh * R.imult + (size_t)g.yh * R.jmult) * hb;
+  ST3D_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + off, R.imult * hb,
+                              static_cast<const char*>(c->stage) + off, R.imult * hb,
+                              (size_t)g.ys * R.jmult * hb, g.xs, cudaMemcpyDeviceToHost, c->stream));
   return ST3D_OK;
 }
 
@@ -533,6 +611,7 @@ int st3d_destroy(st3d_ctx* c) {
   if (c->scratch) cudaFree(c->scratch);
   if (c->counter) cudaFree(c->counter);
   if (c->dev_status) cudaFree(c->dev_status);
+  if (c->stage) cudaFree(c->stage);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -574,15 +653,15 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   int rc;
   if (u) {
-    if ((rc = copy_field(c, u_ptr(c), const_cast<void*>(u), true, true)) != ST3D_OK) return rc;
+    if ((rc = upload_field(c, u_ptr(c), u)) != ST3D_OK) return rc;
     c->has_u = true;
   }
   if (v) {
-    if ((rc = copy_field(c, v_ptr(c), const_cast<void*>(v), true, true)) != ST3D_OK) return rc;
+    if ((rc = upload_field(c, v_ptr(c), v)) != ST3D_OK) return rc;
     c->has_v = true;
   }
   if (s) {
-    if ((rc = copy_field(c, c->fld[2], const_cast<void*>(s), true, true)) != ST3D_OK) return rc;
+    if ((rc = upload_field(c, c->fld[2], s)) != ST3D_OK) return rc;
     c->has_s = true;
   }
   c->step = 0;
@@ -592,8 +671,8 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
 int st3d_download(st3d_ctx* c, void* v, void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   int rc;
-  if (v && (rc = copy_field(c, v_ptr(c), v, false, false)) != ST3D_OK) return rc;
-  if (u && (rc = copy_field(c, u_ptr(c), u, false, false)) != ST3D_OK) return rc;
+  if (v && (rc = download_field(c, v_ptr(c), v)) != ST3D_OK) return rc;
+  if (u && (rc = download_field(c, u_ptr(c), u)) != ST3D_OK) return rc;
   ST3D_CUDA(cudaStreamSynchronize(c->stream));
   return ST3D_OK;
 }

@@ -86,6 +86,12 @@ inline Geom geom_of(const Layout& L) {
   return g;
 }
 
+// The caller's reference layout (grid.cpp:20-24).
+struct RefGeom {
+  int xs, ys, zs;
+  long long jmult, imult, ijk_ofs;
+};
+
 // Mode W point source for one step.
 struct Source {
   int i, j, k;   // interior coordinates; i < 0: none
@@ -117,6 +123,12 @@ cudaError_t launch_tma(const TmaPlan& plan, int points, int mode, const Geom& g,
 bool tma_config_supported(int tj, int nv);
 // Resident CTAs per SM of the TMA kernel for this configuration (0: cannot run).
 int tma_blocks_per_sm(int points, int mode, int tj, int nv, size_t smem);
+
+// Reference layout (staging buffer) <-> library layout, element size eb.
+cudaError_t launch_ref_to_dev(int eb, const Layout& L, const RefGeom& R, const void* stage,
+                              void* dst, int hx, int hy, int hz, cudaStream_t stream);
+cudaError_t launch_dev_to_ref(int eb, const Layout& L, const RefGeom& R, const void* src,
+                              void* stage, int hz, cudaStream_t stream);
 
 cudaError_t launch_fill(int storage, const Layout& L, void* dst, int kind, uint64_t seed,
                         unsigned field, double a, double b, const double* blob_params, int nblobs,
