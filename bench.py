@@ -64,38 +64,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target CPU time of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--precision-forms", default="f16_hilo,f16,bf16",
+                   help="16-bit storage forms timed and judged against FP64 ('' to skip)")
     return p.parse_args()
-
-
-# --------------------------------------------------------------------------
-# distributed plumbing (replicas only)
-# --------------------------------------------------------------------------
-class Dist:
-    def __init__(self):
-        self.world = int(os.environ.get("WORLD_SIZE", "1"))
-        self.rank = int(os.environ.get("RANK", "0"))
-        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-        self.pg = None
-        if self.world > 1:
-            import torch.distributed as td
-            td.init_process_group("gloo")
-            self.td = td
-
-    def barrier(self):
-        if self.world > 1:
-            self.td.barrier()
-
-    def max(self, x):
-        if self.world == 1:
-            return x
-        import torch
-        t = torch.tensor([float(x)], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
-        return float(t.item())
-
-    def close(self):
-        if self.world > 1:
-            self.td.destroy_process_group()
 
 
 # --------------------------------------------------------------------------
@@ -194,26 +165,44 @@ def init_fields(S, st, init):
     st.synchronize()
 
 
-def accuracy_run(S, wl, steps, kernel):
-    """FP32 and FP64 runs of the same workload; relative L2 and max error of
-    u against FP64 every 100 steps (FP64 reductions on the device)."""
-    g, a = make_stencil(S, wl, "f32", kernel)
-    _, b = make_stencil(S, wl, "f64")
-    report = []
+def accuracy_run(S, wl, steps, kernel, storages):
+    """Runs of the same workload in each storage next to an FP64 run; relative
+    L2 and max error of u against FP64 every 100 steps (FP64 device
+    reductions)."""
+    ref_g, ref = make_stencil(S, wl, "f64")
+    runs = {st: make_stencil(S, wl, st, kernel if st == "f32" else "auto")[1] for st in storages}
+    report = {st: [] for st in storages}
     done = 0
     while done < steps:
         n = min(100, steps - done)
-        a.iterate(n)
-        b.iterate(n)
-        a.synchronize()
-        b.synchronize()
+        ref.iterate(n)
+        for st in storages:
+            runs[st].iterate(n)
+        ref.synchronize()
         done += n
-        d2, b2, dm, bm = a.norms(S.FIELD_U, b, S.FIELD_U)
-        report.append({"step": done, "rel_l2": (d2 / b2) ** 0.5 if b2 > 0 else None,
-                       "max_abs": dm, "rel_max": dm / bm if bm > 0 else None})
-    a.close()
-    b.close()
+        for st in storages:
+            runs[st].synchronize()
+            d2, b2, dm, bm = runs[st].norms(S.FIELD_U, ref, S.FIELD_U)
+            report[st].append({"step": done, "rel_l2": (d2 / b2) ** 0.5 if b2 > 0 else None,
+                               "max_abs": dm, "rel_max": dm / bm if bm > 0 else None})
+    for r in runs.values():
+        r.close()
+    ref.close()
     return report
+
+
+def time_storage(S, wl, storage, steps, warmup, kernel="auto"):
+    """Device time of `steps` steps in one storage (fresh fields, W warm-up)."""
+    g, st = make_stencil(S, wl, storage, kernel)
+    info = st.info()
+    st.iterate(warmup)
+    st.synchronize()
+    st.timer_start()
+    st.iterate(steps)
+    ms = st.timer_stop()
+    st.synchronize()
+    st.close()
+    return g.gvol * steps / (ms * 1e-3) / 1e9, ms / steps, info
 
 
 def e2e_run(S, st, g, calls, iters):
@@ -230,6 +219,17 @@ def e2e_run(S, st, g, calls, iters):
             st.timer_start()
             st.iterate_host(pv.array, ps.array, pu.array, iters)
             times.append(st.timer_stop())
+        # the same call split into its phases, for the record
+        phases = {}
+        st.timer_start()
+        st.upload(pv.array, ps.array, pu.array)
+        phases["upload_ms"] = st.timer_stop()
+        st.timer_start()
+        st.iterate(iters)
+        phases["iterate_ms"] = st.timer_stop()
+        st.timer_start()
+        st.download(pv.array, pu.array)
+        phases["download_ms"] = st.timer_stop()
         host = (pv.array.copy(), pu.array.copy())
     finally:
         for p in (pv, ps, pu):
@@ -244,7 +244,9 @@ def e2e_run(S, st, g, calls, iters):
     return {"value": pts * iters / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "step": "one ITERATE-equivalent call (st3d_iterate_host) of %d time steps" % iters,
-            "ms_per_call": ms}, host
+            "ms_per_call": ms, "phases": phases,
+            "h2d_gbs": h2d / (phases["upload_ms"] * 1e-3) / 1e9,
+            "d2h_gbs": d2h / (phases["download_ms"] * 1e-3) / 1e9}, host
 
 
 def cpu_wave_sample(wl, u, v, target_s, threads):
@@ -333,10 +335,25 @@ def run_gb300(args, dist):
         "fp16": None,
     }
 
+    forms = [f for f in args.precision_forms.split(",") if f]
+    if forms:
+        result["fp16"] = {}
+        for form in forms:
+            gp, msf, finfo = time_storage(S, args.workload, form, args.steps, args.warmup)
+            gp = dist.world * gp * (ms / ms_max)  # same replica scaling as value
+            ach = finfo.bytes_per_point * pts / (msf * 1e-3) / 1e9
+            result["fp16"][form] = {"value": gp, "unit": "Gpts/s", "ms_per_step": msf,
+                                    "speedup_vs_fp32": gp / value,
+                                    "bytes_per_point": finfo.bytes_per_point,
+                                    "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
+                                                 "frac": ach / peak}}
     if dist.rank == 0 and args.accuracy_steps > 0:
-        result["accuracy_vs_fp64"] = accuracy_run(S, args.workload, args.accuracy_steps,
-                                                  args.kernel)
-        result["l2_err_fp32_vs_fp64"] = result["accuracy_vs_fp64"][-1]["rel_l2"]
+        acc = accuracy_run(S, args.workload, args.accuracy_steps, args.kernel, ["f32"] + forms)
+        result["accuracy_vs_fp64"] = acc["f32"]
+        result["l2_err_fp32_vs_fp64"] = acc["f32"][-1]["rel_l2"]
+        for form in forms:
+            result["fp16"][form]["accuracy_vs_fp64"] = acc[form]
+            result["fp16"][form]["l2_err_vs_fp64"] = acc[form][-1]["rel_l2"]
 
     host = None
     if args.e2e_calls > 0:
@@ -406,7 +423,8 @@ def run_reference(args, dist):
 
 def main():
     args = parse()
-    dist = Dist()
+    from stencil3d_gb300.replicas import Replicas
+    dist = Replicas()
     try:
         if args.impl == "reference":
             run_reference(args, dist)

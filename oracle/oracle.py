@@ -224,3 +224,76 @@ def ref_iterate(v, s, u, grid, points, iterations, traversal="2d_jk_blocked"):
     fn = L.ref_iterate if traversal == "2d_jk_blocked" else L.ref_iterate_3d
     fn(v, s, u, *[int(x) for x in grid], iterations)
     return v
+
+
+# ---------------------------------------------------------------------------
+# 16-bit storage forms (FP16 / BF16 words with per-plane scales, optional
+# compensating byte), restated in oracle/st3d_oracle.c
+# ---------------------------------------------------------------------------
+_u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
+_i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+
+def _lib16():
+    L = lib()
+    if not getattr(L, "_f16_ready", False):
+        L.orc16_encode.argtypes = [C.c_int, C.c_int, _f32p, _u32p, _u16p, C.c_void_p, _i32p, _f32p]
+        L.orc16_decode.argtypes = [C.c_int, C.c_int, _u16p, C.c_void_p, _i32p, _u32p, _f32p]
+        L.orc16_iterate_wave.argtypes = [
+            C.c_int, C.c_int, _u16p, C.c_void_p, _i32p, _f32p, _u16p, C.c_void_p, _i32p, _f32p,
+            _u16p, _i32p, _f32p, _u32p, C.c_int, _f32p, C.c_float, C.c_float, C.c_float,
+            C.c_void_p, C.c_void_p, C.c_uint]
+        L.orc16_iterate_wave.restype = C.c_int
+        L.orc16_scale_exponent.argtypes = [C.c_float]
+        L.orc16_scale_exponent.restype = C.c_int
+        L._f16_ready = True
+    return L
+
+
+class Field16:
+    """A field in 16-bit storage: words h, bytes q (compensated form), per-plane
+    scale exponents E and maxima M."""
+
+    def __init__(self, x, grid, kind, hilo):
+        self.kind, self.hilo, self.grid = kind, hilo, grid
+        self.h = np.zeros(shape(grid), np.uint16)
+        self.q = np.zeros(shape(grid), np.int8) if hilo else None
+        self.E = np.zeros(grid[0], np.int32)
+        self.M = np.zeros(grid[0], np.float32)
+        _lib16().orc16_encode(kind, int(hilo), np.ascontiguousarray(x, np.float32), gvec(grid),
+                              self.h, self.q.ctypes.data if hilo else None, self.E, self.M)
+
+    def decode(self):
+        x = np.zeros(shape(self.grid), np.float32)
+        _lib16().orc16_decode(self.kind, int(self.hilo), self.h,
+                              self.q.ctypes.data if self.hilo else None, self.E,
+                              gvec(self.grid), x)
+        return x
+
+
+def storage_kind(storage):
+    """(kind, hilo) of a 16-bit storage name."""
+    return {"f16": (0, False), "bf16": (1, False), "f16_hilo": (0, True)}[storage]
+
+
+def k4_of(points, c1):
+    """4*c1*sum(w) rounded to float, as the library forms it."""
+    w = wave_weights(points)
+    return float(np.float32(4.0 * c1 * sum(float(x) for x in w[2:14])))
+
+
+def iterate_wave16(u, v, s, grid, points, iterations, c1, c2, src=None, amps=None, weights=None):
+    """Mode W on Field16 states u, v (in place; u newest afterwards) and s."""
+    if weights is None:
+        weights = wave_weights(points)
+    srcv = None if src is None else np.asarray(src, dtype=np.int64)
+    ampv = None if amps is None else np.ascontiguousarray(amps, dtype=np.float32)
+    rc = _lib16().orc16_iterate_wave(
+        u.kind, int(u.hilo), u.h, u.q.ctypes.data if u.hilo else None, u.E, u.M,
+        v.h, v.q.ctypes.data if v.hilo else None, v.E, v.M, s.h, s.E, s.M, gvec(grid), points,
+        np.ascontiguousarray(weights, np.float32), c1, c2, k4_of(points, c1),
+        srcv.ctypes.data if srcv is not None else None,
+        ampv.ctypes.data if ampv is not None else None, iterations)
+    assert rc == 0, rc
+    return u, v

@@ -474,3 +474,230 @@ double orc_ricker(double t, double f, double t0) {
 DEFINE_DIFF(f32_f32, float, float)
 DEFINE_DIFF(f32_f64, float, double)
 DEFINE_DIFF(f64_f64, double, double)
+
+/* ------------------------------------------------------------------ */
+/* 16-bit storage forms of mode W                                      */
+/* ------------------------------------------------------------------ */
+/*
+ * Restates the precision form of the library (no reference code exists):
+ * a field is a 16-bit word per point (FP16 kind 0 or BF16 kind 1, round to
+ * nearest even) with a power-of-two scale 2^E per i-plane, plus, in the
+ * compensated form (hilo), a signed byte q holding the residual in units of
+ * ulp(h)/256:  x = (h + q*ulp(h)/256) * 2^E.  One step decodes u (neighbour
+ * terms from the word alone, the centre from word + byte), v and s, applies
+ * the FP32 fused difference-form update, and encodes the new field with the
+ * scale E = floor(log2 B) - 13 of the bound
+ *   B = 3*max(Mu[i], Mv[i]) + k4*max_{|d|<=R} Mu[i+d] + c2*(Ms[i] + |a_n|*[i == src_i]),
+ * M = per-plane maxima of |U^n|, |U^{n-1}|, |s| (of the values before
+ * encoding).  Arrays are in the reference layout; halos must be zero.
+ */
+static inline uint16_t f32_to_f16(float x) {
+  _Float16 h = (_Float16)x;
+  uint16_t b;
+  memcpy(&b, &h, 2);
+  return b;
+}
+static inline float f16_to_f32(uint16_t b) {
+  _Float16 h;
+  memcpy(&h, &b, 2);
+  return (float)h;
+}
+static inline uint16_t f32_to_bf16(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+static inline float bf16_to_f32(uint16_t b) {
+  uint32_t u = (uint32_t)b << 16;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+static inline float exp2i_f(int e) {
+  uint32_t u = (uint32_t)(e + 127) << 23;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+static inline float ulp256(uint16_t hb) {
+  int e = (hb >> 10) & 0x1f;
+  if (e == 0) e = 1;
+  return exp2i_f(e - 33);
+}
+int orc16_scale_exponent(float B) {
+  if (!(B > 0.0f) || !(B < 3.0e38f)) return -100;
+  uint32_t u;
+  memcpy(&u, &B, 4);
+  const int e = (int)((u >> 23) & 0xff);
+  if (e == 0) return -100;
+  int E = (e - 127) - 13;
+  return E < -100 ? -100 : (E > 100 ? 100 : E);
+}
+static inline float w2f(int kind, uint16_t b) { return kind ? bf16_to_f32(b) : f16_to_f32(b); }
+static inline uint16_t f2w(int kind, float x) { return kind ? f32_to_bf16(x) : f32_to_f16(x); }
+
+static inline float dec16(int kind, int hilo, uint16_t h, int8_t q, int E) {
+  float x = w2f(kind, h);
+  if (hilo) x = fmaf((float)q, ulp256(h), x);
+  return x * exp2i_f(E);
+}
+static inline void enc16(int kind, int hilo, float x, int E, uint16_t* h, int8_t* q) {
+  const float xs = x * exp2i_f(-E);
+  *h = f2w(kind, xs);
+  if (hilo) {
+    const float r = xs - w2f(kind, *h);
+    int e = (*h >> 10) & 0x1f;
+    if (e == 0) e = 1;
+    long qi = lrintf(r * exp2i_f(33 - e));
+    if (qi > 127) qi = 127;
+    if (qi < -127) qi = -127;
+    *q = (int8_t)qi;
+  }
+}
+
+/* Encode a float field (reference layout) into 16-bit storage: plane maxima
+ * M (interior), scales E, words h and bytes q (q may be NULL). */
+void orc16_encode(int kind, int hilo, const float* x, const unsigned* g, uint16_t* h, int8_t* q,
+                  int* E, float* M) {
+  const orc_layout L = mk_layout(g);
+  for (unsigned i = 0; i < L.xs; i++) {
+    float m = 0.0f;
+    for (unsigned j = 0; j < L.ys; j++)
+      for (unsigned k = 0; k < L.zs; k++) {
+        const float a = fabsf(x[L.ijk_ofs + (size_t)i * L.imult + (size_t)j * L.jmult + k]);
+        if (a > m) m = a;
+      }
+    M[i] = m;
+    E[i] = orc16_scale_exponent(m);
+  }
+  const long long ni = L.xs + 2 * L.xh, nj = L.ys + 2 * L.yh, nk = L.zs + 2 * L.zh;
+  for (long long ii = 0; ii < ni; ii++) {
+    const long long i = ii - L.xh;
+    const int e = (i >= 0 && i < (long long)L.xs) ? E[i] : 0;
+    for (long long jj = 0; jj < nj; jj++)
+      for (long long kk = 0; kk < nk; kk++) {
+        const size_t p = (size_t)ii * L.imult + (size_t)jj * L.jmult + (size_t)kk;
+        int8_t qq = 0;
+        enc16(kind, hilo && q, x[p], e, &h[p], &qq);
+        if (q) q[p] = qq;
+      }
+  }
+}
+
+/* Decode the interior of a 16-bit field into float (halos left as they are). */
+void orc16_decode(int kind, int hilo, const uint16_t* h, const int8_t* q, const int* E,
+                  const unsigned* g, float* x) {
+  const orc_layout L = mk_layout(g);
+  for (unsigned i = 0; i < L.xs; i++)
+    for (unsigned j = 0; j < L.ys; j++)
+      for (unsigned k = 0; k < L.zs; k++) {
+        const size_t p = L.ijk_ofs + (size_t)i * L.imult + (size_t)j * L.jmult + k;
+        x[p] = dec16(kind, hilo && q, h[p], q ? q[p] : 0, E[i]);
+      }
+}
+
+/* `iterations` steps; on return the u arrays hold U^{n+it} and the v arrays
+ * U^{n+it-1} (contents swapped back after an odd count). */
+int orc16_iterate_wave(int kind, int hilo, uint16_t* uh, int8_t* uq, int* uE, float* uM,
+                       uint16_t* vh, int8_t* vq, int* vE, float* vM, const uint16_t* sh,
+                       const int* sE, const float* sM, const unsigned* g, int points,
+                       const float* c, float c1, float c2, float k4, const long long* src,
+                       const float* amp, unsigned iterations) {
+  const orc_layout L = mk_layout(g);
+  const int R = radius_of(points);
+  if (R < 0 || points == 2) return 1;
+  int axis[12], rad[12];
+  const int np = pair_order(points, axis, rad);
+  long long off_m[12], off_p[12];
+  float cf[12];
+  for (int p = 0; p < np; p++) {
+    const long long st = axis[p] == 0 ? (long long)L.imult : axis[p] == 1 ? (long long)L.jmult : 1;
+    off_m[p] = -st * rad[p];
+    off_p[p] = st * rad[p];
+    cf[p] = c[2 + 4 * axis[p] + rad[p] - 1];
+  }
+  const int si = (src && src[0] >= 0) ? (int)src[0] : -1;
+  const long long src_x = si >= 0 ? (long long)(L.ijk_ofs + (size_t)src[0] * L.imult +
+                                                (size_t)src[1] * L.jmult + (size_t)src[2])
+                                  : -1;
+  int* Eout = (int*)malloc(L.xs * sizeof(int));
+  float* Mout = (float*)malloc(L.xs * sizeof(float));
+  if (!Eout || !Mout) return 2;
+  uint16_t *Uh = uh, *Vh = vh;
+  int8_t *Uq = uq, *Vq = vq;
+  int *UE = uE, *VE = vE;
+  float *UM = uM, *VM = vM;
+  for (unsigned it = 0; it < iterations; it++) {
+    const float a = amp ? amp[it] : 0.0f;
+    for (unsigned i = 0; i < L.xs; i++) {
+      float nb = 0.0f;
+      for (int d = -R; d <= R; d++) {
+        const long long ii = (long long)i + d;
+        if (ii >= 0 && ii < (long long)L.xs) nb = fmaxf(nb, UM[ii]);
+      }
+      float B = 3.0f * fmaxf(UM[i], VM[i]);
+      B = B + k4 * nb;
+      B = B + c2 * (sM[i] + ((int)i == si ? fabsf(a) : 0.0f));
+      Eout[i] = orc16_scale_exponent(B);
+      Mout[i] = 0.0f;
+    }
+#pragma omp parallel for schedule(static)
+    for (unsigned i = 0; i < L.xs; i++) {
+      float m = 0.0f;
+      for (unsigned j = 0; j < L.ys; j++)
+        for (unsigned k = 0; k < L.zs; k++) {
+          const size_t x = L.ijk_ofs + (size_t)i * L.imult + (size_t)j * L.jmult + k;
+          /* neighbour words decode with their own plane's scale; halo planes
+             are zero whatever their scale */
+          float nbv_m[12], nbv_p[12];
+          for (int p = 0; p < np; p++) {
+            long long im = i, ip = i;
+            if (axis[p] == 0) { im = (long long)i - rad[p]; ip = (long long)i + rad[p]; }
+            const int em = (im >= 0 && im < (long long)L.xs) ? UE[im] : 0;
+            const int ep = (ip >= 0 && ip < (long long)L.xs) ? UE[ip] : 0;
+            nbv_m[p] = w2f(kind, Uh[x + off_m[p]]) * exp2i_f(em);
+            nbv_p[p] = w2f(kind, Uh[x + off_p[p]]) * exp2i_f(ep);
+          }
+          const float u0 = dec16(kind, hilo, Uh[x], hilo ? Uq[x] : 0, UE[i]);
+          const float v0 = dec16(kind, hilo, Vh[x], hilo ? Vq[x] : 0, VE[i]);
+          float s0 = dec16(kind, 0, sh[x], 0, sE[i]);
+          if ((long long)x == src_x) s0 = s0 + a;
+          const float u2 = u0 + u0;
+          float lap = cf[0] * ((nbv_m[0] + nbv_p[0]) - u2);
+          for (int p = 1; p < np; p++) lap = fmaf(cf[p], (nbv_m[p] + nbv_p[p]) - u2, lap);
+          float t = u2 - v0;
+          t = fmaf(c1, lap, t);
+          const float out = fmaf(c2, s0, t);
+          int8_t qq = 0;
+          enc16(kind, hilo, out, Eout[i], &Vh[x], &qq);
+          if (hilo) Vq[x] = qq;
+          if (fabsf(out) > m) m = fabsf(out);
+        }
+      Mout[i] = m;
+    }
+    memcpy(VE, Eout, L.xs * sizeof(int));
+    memcpy(VM, Mout, L.xs * sizeof(float));
+    { uint16_t* t = Uh; Uh = Vh; Vh = t; }
+    { int8_t* t = Uq; Uq = Vq; Vq = t; }
+    { int* t = UE; UE = VE; VE = t; }
+    { float* t = UM; UM = VM; VM = t; }
+  }
+  free(Eout);
+  free(Mout);
+  if (Uh != uh) {
+    const size_t n = L.gsize;
+    uint16_t* th = (uint16_t*)malloc(n * 2);
+    int8_t* tq = (int8_t*)malloc(n);
+    if (!th || !tq) return 2;
+    memcpy(th, uh, n * 2); memcpy(uh, vh, n * 2); memcpy(vh, th, n * 2);
+    if (hilo) { memcpy(tq, uq, n); memcpy(uq, vq, n); memcpy(vq, tq, n); }
+    for (unsigned i = 0; i < L.xs; i++) {
+      int te = uE[i]; uE[i] = vE[i]; vE[i] = te;
+      float tm = uM[i]; uM[i] = vM[i]; vM[i] = tm;
+    }
+    free(th);
+    free(tq);
+  }
+  return 0;
+}

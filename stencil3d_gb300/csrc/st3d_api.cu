@@ -17,6 +17,7 @@
 #include <new>
 #include <string>
 
+#include "st3d_f16.cuh"
 #include "st3d_internal.h"
 #include "st3d_tma.cuh"
 
@@ -62,6 +63,16 @@ int elem_bytes(int storage) {
 }
 
 int host_elem_bytes(int storage) { return storage == ST3D_F64 ? 8 : 4; }
+
+// Algorithmic HBM bytes per point per step: read u, v, s and write v
+// (config.h:76,82,88 count these 4 streams); 2 points read u and write v
+// (config.h:70).  16-bit storage: 2 bytes per stream (8 B); the compensated
+// form adds the low bytes of the centre u, of v and of the written v (11 B).
+double f16_bytes(int storage, int points, int eb) {
+  if (storage == ST3D_F16_HILO) return 11.0;
+  if (storage == ST3D_F16 || storage == ST3D_BF16) return 8.0;
+  return (points == 2 ? 2.0 : 4.0) * eb;
+}
 
 }  // namespace
 
@@ -134,6 +145,16 @@ struct st3d_ctx {
   bool has_u = false, has_v = false, has_s = false;
   int device = 0;
   TmaPlan* tma = nullptr;
+  // 16-bit storage: low bytes of the u/v buffers (compensated form), scale
+  // exponents (time levels mod 3, then s) and plane maxima (time levels mod 4,
+  // then s), the halo check word, the kernel plan
+  bool f16 = false;
+  void* lo[2] = {nullptr, nullptr};
+  int* E = nullptr;
+  uint32_t* M = nullptr;
+  uint32_t* halo_max = nullptr;
+  Tma16Plan* tma16 = nullptr;
+  float k4 = 0.0f;
   void* stage = nullptr;      // reference-layout staging buffer for host copies
   size_t stage_bytes = 0;
   Coefs<float> cf32;
@@ -169,10 +190,15 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_INVALID, "halo (%u,%u,%u) too wide", g->xh, g->yh, g->zh);
   if (o->mode == ST3D_MODE_WAVE && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the 2-point stencil has no wave form (it is not a Laplacian)");
-  if (o->storage != ST3D_F32 && o->storage != ST3D_F64)
-    return fail(ST3D_ERR_UNSUPPORTED, "storage %d is not available in this build", o->storage);
-  if (o->kernel == ST3D_KERNEL_TMA && o->storage != ST3D_F32)
-    return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves FP32 storage only");
+  const bool s16 = o->storage == ST3D_F16 || o->storage == ST3D_BF16 || o->storage == ST3D_F16_HILO;
+  if (s16 && o->mode != ST3D_MODE_WAVE)
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage is the precision form of the wave update only");
+  if (s16 && o->kernel == ST3D_KERNEL_SIMPLE)
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage runs on the TMA kernel only");
+  if (s16 && (g->xs > 65535 - 8 || g->ys > 65535 - 8 || g->zh > 64))
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage needs xs, ys <= 65527 and zh <= 64");
+  if (o->kernel == ST3D_KERNEL_TMA && o->storage == ST3D_F64)
+    return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves FP32 and 16-bit storage");
   if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves the 7/13/25-point stencils");
   if (o->temporal_block != 0 && o->temporal_block != 1)
@@ -351,6 +377,147 @@ int download_field(st3d_ctx* c, const void* dev, void* host) {
   return ST3D_OK;
 }
 
+int mod(long long a, int m) { return (int)(((a % m) + m) % m); }
+int* E_level(st3d_ctx* c, long long level) { return c->E + (size_t)mod(level, 3) * c->grid.xs; }
+uint32_t* M_level(st3d_ctx* c, long long level) { return c->M + (size_t)mod(level, 4) * c->grid.xs; }
+int* E_s(st3d_ctx* c) { return c->E + 3 * (size_t)c->grid.xs; }
+uint32_t* M_s(st3d_ctx* c) { return c->M + 4 * (size_t)c->grid.xs; }
+
+int encode_map_t(CUtensorMap* m, CUtensorMapDataType dt, int eb, void* base, const Layout& L,
+                 uint32_t box_k, uint32_t box_j, uint32_t kext, uint32_t jext) {
+  auto enc = get_encode();
+  if (!enc) return fail(ST3D_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  cuuint64_t dims[3] = {(cuuint64_t)L.pk + L.zs + kext, (cuuint64_t)L.pj + L.ys + jext, L.ni};
+  cuuint64_t strides[2] = {(cuuint64_t)L.nk * eb, (cuuint64_t)L.nk * L.nj * eb};
+  cuuint32_t box[3] = {box_k, box_j, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(m, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ST3D_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return ST3D_OK;
+}
+
+// 16-bit plan: the FP32 decomposition with 16-bit tiles (8-word k halo).
+int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
+  Tma16Plan* p = new (std::nothrow) Tma16Plan();
+  if (!p) return fail(ST3D_ERR_NOMEM, "host allocation failed");
+  const int R = c->R;
+  const bool hilo = c->opts.storage == ST3D_F16_HILO;
+  p->radius = R;
+  p->tj = 16;
+  p->nv = 3;
+  p->smem = tma16_smem_bytes(p->tj, p->nv, R, hilo);
+  if ((int)p->smem > max_smem) {
+    delete p;
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit kernel needs %zu bytes of shared memory", p->smem);
+  }
+  const int per_sm = tma16_blocks_per_sm(c->opts.storage, c->opts.points, *p);
+  if (per_sm < 1) {
+    delete p;
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit kernel cannot be resident");
+  }
+  p->ntj = (int)((c->L.ys + p->tj - 1) / p->tj);
+  p->ntk = (int)((c->L.zs + 127) / 128);
+  const int ctas = sm_count * per_sm;
+  p->ichunk = c->opts.ichunk > 0 ? c->opts.ichunk : tma_pick_ichunk((int)c->L.xs, p->ntj * p->ntk, ctas, R);
+  p->nti = (int)((c->L.xs + p->ichunk - 1) / p->ichunk);
+  p->units = p->ntj * p->ntk * p->nti;
+  p->grid = ctas < p->units ? ctas : p->units;
+  p->threads = (p->tj + 1) * 32;
+  const CUtensorMapDataType w16 =
+      c->opts.storage == ST3D_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+  int ok = ST3D_OK;
+  for (int f = 0; f < 2 && ok == ST3D_OK; ++f) {
+    ok = encode_map_t(&p->uhi[f], w16, 2, c->fld[f], c->L, 144, p->tj + 2 * R, 8, c->L.pj);
+    if (ok == ST3D_OK) ok = encode_map_t(&p->vhi[f], w16, 2, c->fld[f], c->L, 128, p->tj, 0, 0);
+    if (ok == ST3D_OK && hilo)
+      ok = encode_map_t(&p->lo[f], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, c->lo[f], c->L, 128, p->tj, 0, 0);
+    else if (ok == ST3D_OK)
+      p->lo[f] = p->vhi[f];  // unused by the uncompensated kernels
+  }
+  if (ok == ST3D_OK) ok = encode_map_t(&p->vhi[2], w16, 2, c->fld[2], c->L, 128, p->tj, 0, 0);
+  if (ok != ST3D_OK) {
+    delete p;
+    return ok;
+  }
+  c->tma16 = p;
+  return ST3D_OK;
+}
+
+// Upload of one field into 16-bit storage from a float host array: contiguous
+// copy to the staging buffer, per-plane maxima, encode + scatter with the
+// planes' scales; the halo must be zero.  which: 0 = u (time level 0),
+// 1 = v (time level -1), 2 = s.
+int upload_field16(st3d_ctx* c, int which, const void* host) {
+  int rc = ensure_stage(c);
+  if (rc != ST3D_OK) return rc;
+  if (host)
+    ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyHostToDevice, c->stream));
+  const st3d_grid_desc& g = c->grid;
+  const RefGeom R = ref_geom(g);
+  const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4, hz = (int)g.zh;
+  uint32_t* M = which == 0 ? M_level(c, 0) : which == 1 ? M_level(c, -1) : M_s(c);
+  int* E = which == 0 ? E_level(c, 0) : which == 1 ? E_level(c, -1) : E_s(c);
+  const int buf = which == 2 ? 2 : (which == 0 ? u_index(c) : v_index(c));
+  ST3D_CUDA(cudaMemsetAsync(M, 0, g.xs * sizeof(uint32_t), c->stream));
+  ST3D_CUDA(cudaMemsetAsync(c->halo_max, 0, sizeof(uint32_t), c->stream));
+  cudaError_t e = launch_plane_max_ref(R, (const float*)c->stage, M, c->halo_max, hx, hy, hz, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "plane maximum kernel");
+  const int storage = (which == 2 && c->opts.storage == ST3D_F16_HILO) ? ST3D_F16 : c->opts.storage;
+  e = launch_ref_to_dev16(storage, c->L, R, (const float*)c->stage, (uint16_t*)c->fld[buf],
+                          which == 2 ? nullptr : (int8_t*)c->lo[buf], M, E, hx, hy, hz, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "16-bit encode kernel");
+  uint32_t halo = 0;
+  ST3D_CUDA(cudaMemcpyAsync(&halo, c->halo_max, sizeof halo, cudaMemcpyDeviceToHost, c->stream));
+  ST3D_CUDA(cudaStreamSynchronize(c->stream));
+  if (halo != 0)
+    return fail(ST3D_ERR_UNSUPPORTED,
+                "16-bit storage needs a zero halo (a zero Dirichlet boundary); field %d has nonzero halo values",
+                which);
+  return ST3D_OK;
+}
+
+int download_field16(st3d_ctx* c, int which, void* host) {
+  int rc = ensure_stage(c);
+  if (rc != ST3D_OK) return rc;
+  const st3d_grid_desc& g = c->grid;
+  const RefGeom R = ref_geom(g);
+  const long long level = which == 0 ? (long long)c->step : (long long)c->step - 1;
+  const int buf = which == 0 ? u_index(c) : v_index(c);
+  cudaError_t e = launch_dev16_to_ref(c->opts.storage, c->L, R, (const uint16_t*)c->fld[buf],
+                                      (const int8_t*)c->lo[buf], E_level(c, level), (float*)c->stage,
+                                      (int)g.zh, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "16-bit decode kernel");
+  const size_t off = ((size_t)g.xh * R.imult + (size_t)g.yh * R.jmult) * 4;
+  ST3D_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + off, R.imult * 4,
+                              static_cast<const char*>(c->stage) + off, R.imult * 4,
+                              (size_t)g.ys * R.jmult * 4, g.xs, cudaMemcpyDeviceToHost, c->stream));
+  return ST3D_OK;
+}
+
+FieldRef field_ref(st3d_ctx* c, int f) {
+  FieldRef r;
+  r.storage = c->opts.storage;
+  r.lo = nullptr;
+  r.E = nullptr;
+  if (f == ST3D_FIELD_S) {
+    r.p = c->fld[2];
+    if (c->f16) {
+      r.E = E_s(c);
+      if (r.storage == ST3D_F16_HILO) r.storage = ST3D_F16;
+    }
+    return r;
+  }
+  const int buf = f == ST3D_FIELD_U ? u_index(c) : v_index(c);
+  r.p = c->fld[buf];
+  if (c->f16) {
+    r.E = E_level(c, f == ST3D_FIELD_U ? (long long)c->step : (long long)c->step - 1);
+    if (r.storage == ST3D_F16_HILO) r.lo = (const int8_t*)c->lo[buf];
+  }
+  return r;
+}
+
 int check_device_status(st3d_ctx* c) {
   uint32_t st = 0;
   ST3D_CUDA(cudaMemcpyAsync(&st, c->dev_status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
@@ -496,11 +663,12 @@ int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info
   info->nk = L.nk; info->nj = L.nj; info->ni = L.ni;
   info->pk = L.pk; info->pj = L.pj; info->pi = L.pi;
   info->radius = R;
-  info->bytes_per_point = (opts->points == 2 ? 2.0 : 4.0) * eb;
+  info->bytes_per_point = f16_bytes(opts->storage, opts->points, eb);
   info->flops_per_point = opts->points == 2 ? 2 : opts->points == 7 ? 12 : opts->points == 13 ? 29 : 41;
   const int tj = opts->tile_j > 0 ? opts->tile_j : 16;
-  const bool tma = opts->storage == ST3D_F32 && opts->points != 2 &&
-                   opts->kernel != ST3D_KERNEL_SIMPLE && tma_config_supported(tj, 3);
+  const bool f16 = eb == 2;
+  const bool tma = f16 || (opts->storage == ST3D_F32 && opts->points != 2 &&
+                           opts->kernel != ST3D_KERNEL_SIMPLE && tma_config_supported(tj, 3));
   info->kernel = tma ? ST3D_KERNEL_TMA : ST3D_KERNEL_SIMPLE;
   info->tile_j = tma ? tj : 0;
   info->tile_k = tma ? kTmaTK : 0;
@@ -569,8 +737,39 @@ int st3d_create(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_ctx** ou
       return cleanup(fail(ST3D_ERR_CUDA, "cudaMemsetAsync failed"));
   cudaMemsetAsync(c->dev_status, 0, sizeof(uint32_t), c->stream);
 
+  c->f16 = c->eb == 2;
+  if (c->f16) {
+    const size_t xs = grid->xs;
+    bool okm = true;
+    if (c->opts.storage == ST3D_F16_HILO)
+      for (int f = 0; f < 2; ++f) {
+        okm = okm && cudaMalloc(&c->lo[f], c->L.elems()) == cudaSuccess;
+        if (okm) {
+          c->bytes += c->L.elems();
+          cudaMemsetAsync(c->lo[f], 0, c->L.elems(), c->stream);
+        }
+      }
+    okm = okm && cudaMalloc(&c->E, 4 * xs * sizeof(int)) == cudaSuccess &&
+          cudaMalloc(&c->M, 5 * xs * sizeof(uint32_t)) == cudaSuccess &&
+          cudaMalloc(&c->halo_max, sizeof(uint32_t)) == cudaSuccess;
+    if (!okm) {
+      cudaGetLastError();
+      return cleanup(fail(ST3D_ERR_NOMEM, "cudaMalloc of the 16-bit storage buffers failed"));
+    }
+    cudaMemsetAsync(c->E, 0, 4 * xs * sizeof(int), c->stream);
+    cudaMemsetAsync(c->M, 0, 5 * xs * sizeof(uint32_t), c->stream);
+    double wsum = 0.0;
+    for (int m = 2; m < 14; ++m) wsum += c->opts.coef[m];
+    c->k4 = (float)(4.0 * c->opts.c1 * wsum);
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    rc = plan_tma16(c, sm, max_smem);
+    if (rc != ST3D_OK) return cleanup(rc);
+    c->kernel = ST3D_KERNEL_TMA;
+  }
+
   // kernel choice
-  c->kernel = ST3D_KERNEL_SIMPLE;
+  if (!c->f16) c->kernel = ST3D_KERNEL_SIMPLE;
   c->ichunk = c->opts.ichunk > 0 ? c->opts.ichunk : 64;
   if (c->opts.storage == ST3D_F32 && c->opts.points != 2 && c->opts.kernel != ST3D_KERNEL_SIMPLE) {
     int max_smem = 0;
@@ -612,6 +811,12 @@ int st3d_destroy(st3d_ctx* c) {
   if (c->counter) cudaFree(c->counter);
   if (c->dev_status) cudaFree(c->dev_status);
   if (c->stage) cudaFree(c->stage);
+  for (int f = 0; f < 2; ++f)
+    if (c->lo[f]) cudaFree(c->lo[f]);
+  if (c->E) cudaFree(c->E);
+  if (c->M) cudaFree(c->M);
+  if (c->halo_max) cudaFree(c->halo_max);
+  delete c->tma16;
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -631,14 +836,11 @@ int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
   info->pk = c->L.pk; info->pj = c->L.pj; info->pi = c->L.pi;
   info->kernel = c->kernel;
   info->radius = c->R;
-  // Algorithmic bytes per point per step: read u, v, s and write v
-  // (config.h:76,82,88 MEM_BYTES_PER_STENCIL counts the 3 streams + 1
-  // store); 2 points read u and write v (config.h:70).
-  info->bytes_per_point = (c->opts.points == 2 ? 2.0 : 4.0) * c->eb;
+  info->bytes_per_point = f16_bytes(c->opts.storage, c->opts.points, c->eb);
   info->flops_per_point = c->opts.points == 2 ? 2 : c->opts.points == 7 ? 12 : c->opts.points == 13 ? 29 : 41;
-  info->tile_j = c->tma ? c->tma->tj : 0;
-  info->tile_k = c->tma ? kTmaTK : 0;
-  info->ichunk = c->tma ? c->tma->ichunk : c->ichunk;
+  info->tile_j = c->tma ? c->tma->tj : c->tma16 ? c->tma16->tj : 0;
+  info->tile_k = (c->tma || c->tma16) ? kTmaTK : 0;
+  info->ichunk = c->tma ? c->tma->ichunk : c->tma16 ? c->tma16->ichunk : c->ichunk;
   info->temporal_block = c->opts.temporal_block;
   return ST3D_OK;
 }
@@ -652,6 +854,24 @@ int st3d_get_stream(const st3d_ctx* c, void** s) {
 int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   int rc;
+  if (c->f16) {
+    c->step = 0;
+    if (u) {
+      if ((rc = upload_field16(c, 0, u)) != ST3D_OK) return rc;
+      c->has_u = true;
+    }
+    if (v) {
+      if ((rc = upload_field16(c, 1, v)) != ST3D_OK) return rc;
+      c->has_v = true;
+    }
+    if (s) {
+      if ((rc = upload_field16(c, 2, s)) != ST3D_OK) return rc;
+      c->has_s = true;
+    }
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, 1), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, 2), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+    return ST3D_OK;
+  }
   if (u) {
     if ((rc = upload_field(c, u_ptr(c), u)) != ST3D_OK) return rc;
     c->has_u = true;
@@ -671,6 +891,12 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
 int st3d_download(st3d_ctx* c, void* v, void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   int rc;
+  if (c->f16) {
+    if (v && (rc = download_field16(c, 1, v)) != ST3D_OK) return rc;
+    if (u && (rc = download_field16(c, 0, u)) != ST3D_OK) return rc;
+    ST3D_CUDA(cudaStreamSynchronize(c->stream));
+    return ST3D_OK;
+  }
   if (v && (rc = download_field(c, v_ptr(c), v)) != ST3D_OK) return rc;
   if (u && (rc = download_field(c, u_ptr(c), u)) != ST3D_OK) return rc;
   ST3D_CUDA(cudaStreamSynchronize(c->stream));
@@ -691,7 +917,26 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
       src.amp = (float)src.amp_d;
     }
     cudaError_t e;
-    if (c->kernel == ST3D_KERNEL_TMA) {
+    if (c->f16) {
+      const long long n = (long long)c->step;
+      Tma16Step st;
+      st.vout = (uint16_t*)v_ptr(c);
+      st.vlo_out = (int8_t*)c->lo[v_index(c)];
+      st.Eu = E_level(c, n);
+      st.Ev = E_level(c, n - 1);
+      st.Es = E_s(c);
+      st.Eout = E_level(c, n + 1);
+      st.Mu = M_level(c, n);
+      st.Mv = M_level(c, n - 1);
+      st.Ms = M_s(c);
+      st.Mout = M_level(c, n + 1);
+      st.Mzero = M_level(c, n + 2);
+      st.k4 = c->k4;
+      st.ubuf = u_index(c);
+      st.vbuf = v_index(c);
+      e = launch_tma16(c->opts.storage, c->opts.points, *c->tma16, c->G, c->cf32, st, src,
+                       c->dev_status, c->stream);
+    } else if (c->kernel == ST3D_KERNEL_TMA) {
       e = launch_tma(*c->tma, c->opts.points, c->opts.mode, c->G, c->cf32, (float*)v_ptr(c),
                      u_index(c), v_index(c), 2, src, c->dev_status, c->stream);
     } else {
@@ -754,9 +999,29 @@ int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double 
       bp[4 * q + 3] = 2.0 * unit(4 * q + 3) - 1.0;
     }
   }
-  cudaError_t e = launch_fill(c->opts.storage, c->L, dst, kind, seed, (unsigned)field, a, b, bp, nb,
-                              c->stream);
-  if (e != cudaSuccess) return cuda_fail(e, "fill kernel launch");
+  if (c->f16) {
+    // fill the float staging buffer (reference layout, interior only: the
+    // 16-bit forms keep a zero halo), then encode like an upload
+    int rc = ensure_stage(c);
+    if (rc != ST3D_OK) return rc;
+    const st3d_grid_desc& g = c->grid;
+    Layout Lr;
+    Lr.xs = g.xs; Lr.ys = g.ys; Lr.zs = g.zs;
+    Lr.pk = g.zh; Lr.pj = g.yh; Lr.pi = g.xh;
+    Lr.nk = g.zs + 2 * g.zh; Lr.nj = g.ys + 2 * g.yh; Lr.ni = g.xs + 2 * g.xh;
+    cudaError_t e = launch_fill(ST3D_F32, Lr, c->stage, kind, seed, (unsigned)field, a, b, bp, nb, 1,
+                                c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "fill kernel launch");
+    const int which = field == ST3D_FIELD_U ? 0 : field == ST3D_FIELD_V ? 1 : 2;
+    c->step = 0;
+    if ((rc = upload_field16(c, which, nullptr)) != ST3D_OK) return rc;
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, 1), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, 2), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+  } else {
+    cudaError_t e = launch_fill(c->opts.storage, c->L, dst, kind, seed, (unsigned)field, a, b, bp,
+                                nb, 0, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "fill kernel launch");
+  }
   if (field == ST3D_FIELD_U) c->has_u = true;
   if (field == ST3D_FIELD_V) c->has_v = true;
   if (field == ST3D_FIELD_S) c->has_s = true;
@@ -767,7 +1032,7 @@ int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double 
 int st3d_check(st3d_ctx* c, double expected, double tol, uint64_t* errors) {
   if (!c || !errors) return fail(ST3D_ERR_INVALID, "null argument");
   ST3D_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned long long), c->stream));
-  cudaError_t e = launch_check(c->opts.storage, c->G, v_ptr(c), expected, tol, c->counter, c->stream);
+  cudaError_t e = launch_check(c->G, field_ref(c, ST3D_FIELD_V), expected, tol, c->counter, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "check kernel launch");
   unsigned long long n = 0;
   ST3D_CUDA(cudaMemcpyAsync(&n, c->counter, sizeof n, cudaMemcpyDeviceToHost, c->stream));
@@ -780,14 +1045,14 @@ int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]) {
   if (!a || !out) return fail(ST3D_ERR_INVALID, "null argument");
   if (b && (b->grid.xs != a->grid.xs || b->grid.ys != a->grid.ys || b->grid.zs != a->grid.zs))
     return fail(ST3D_ERR_INVALID, "norms need equal interior sizes");
-  auto fptr = [](st3d_ctx* c, int f) -> void* {
-    return f == ST3D_FIELD_U ? u_ptr(c) : f == ST3D_FIELD_V ? v_ptr(c) : c->fld[2];
-  };
   if (fa < 0 || fa > 2 || (b && (fb < 0 || fb > 2))) return fail(ST3D_ERR_INVALID, "bad field");
   if (b && b->stream != a->stream) ST3D_CUDA(cudaStreamSynchronize(b->stream));
   const int nb = norms_blocks(a->G);
-  cudaError_t e = launch_norms(a->opts.storage, a->G, fptr(a, fa), b ? b->opts.storage : 0,
-                               b ? b->G : a->G, b ? fptr(b, fb) : nullptr, a->scratch, nb,
+  FieldRef ra = field_ref(a, fa);
+  FieldRef rb;
+  rb.p = nullptr; rb.storage = 0; rb.lo = nullptr; rb.E = nullptr;
+  if (b) rb = field_ref(b, fb);
+  cudaError_t e = launch_norms(a->G, ra, b ? b->G : a->G, rb, a->scratch, nb,
                                a->scratch + 4 * (size_t)nb, a->stream);
   if (e != cudaSuccess) return cuda_fail(e, "norms kernel launch");
   double h[4];

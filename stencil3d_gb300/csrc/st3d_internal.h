@@ -130,13 +130,56 @@ cudaError_t launch_ref_to_dev(int eb, const Layout& L, const RefGeom& R, const v
 cudaError_t launch_dev_to_ref(int eb, const Layout& L, const RefGeom& R, const void* src,
                               void* stage, int hz, cudaStream_t stream);
 
+// One step of the 16-bit-storage kernel: the output buffer (words and low
+// bytes), the per-plane scale exponents of U^n, U^{n-1}, s and U^{n+1}, the
+// per-plane maxima (float bits) of U^n, U^{n-1}, s, the accumulator of
+// U^{n+1} and the one to clear for U^{n+2}, k4 = 4*c1*sum(w), and which field
+// buffers hold u and v.
+struct Tma16Step {
+  uint16_t* vout;
+  int8_t* vlo_out;
+  const int *Eu, *Ev, *Es;
+  int* Eout;
+  const uint32_t *Mu, *Mv, *Ms;
+  uint32_t *Mout, *Mzero;
+  float k4;
+  int ubuf, vbuf;
+};
+struct Tma16Plan;
+size_t tma16_smem_bytes(int tj, int nv, int R, bool hilo);
+int tma16_blocks_per_sm(int storage, int points, const Tma16Plan& pl);
+cudaError_t launch_tma16(int storage, int points, const Tma16Plan& pl, const Geom& g,
+                         const Coefs<float>& cf, const Tma16Step& st, const Source& src,
+                         uint32_t* dev_status, cudaStream_t stream);
+
+// 16-bit storage transfers (st3d_kernels_copy.cu).
+cudaError_t launch_plane_max_ref(const RefGeom& R, const float* stage, uint32_t* M,
+                                 uint32_t* halo_max, int hx, int hy, int hz, cudaStream_t stream);
+cudaError_t launch_ref_to_dev16(int storage, const Layout& L, const RefGeom& R, const float* stage,
+                                uint16_t* hi, int8_t* lo, const uint32_t* M, int* E, int hx, int hy,
+                                int hz, cudaStream_t stream);
+cudaError_t launch_dev16_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* hi,
+                                const int8_t* lo, const int* E, float* stage, int hz,
+                                cudaStream_t stream);
+
+// interior_only: points outside the interior are set to 0.
 cudaError_t launch_fill(int storage, const Layout& L, void* dst, int kind, uint64_t seed,
                         unsigned field, double a, double b, const double* blob_params, int nblobs,
-                        cudaStream_t stream);
-cudaError_t launch_check(int storage, const Geom& g, const void* v, double expected, double tol,
+                        int interior_only, cudaStream_t stream);
+
+// A device field as the reductions read it: values (float, double or 16-bit
+// words), the low bytes of the compensated form and the per-plane scale
+// exponents of 16-bit storage.
+struct FieldRef {
+  const void* p;
+  int storage;
+  const int8_t* lo;
+  const int* E;
+};
+cudaError_t launch_check(const Geom& g, const FieldRef& v, double expected, double tol,
                          unsigned long long* counter, cudaStream_t stream);
 // Two-pass FP64 reduction: partials of `nblocks` blocks in scratch, then one block.
-cudaError_t launch_norms(int sa, const Geom& ga, const void* a, int sb, const Geom& gb, const void* b,
+cudaError_t launch_norms(const Geom& ga, const FieldRef& a, const Geom& gb, const FieldRef& b,
                          double* scratch, int nblocks, double* out_dev, cudaStream_t stream);
 int norms_blocks(const Geom& g);
 

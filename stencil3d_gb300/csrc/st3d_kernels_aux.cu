@@ -9,6 +9,7 @@
 //    the energy and L2 reductions that judge drift against an FP64 run.
 //    Two passes with per-block partials in a scratch buffer and a fixed
 //    reduction order, so results are deterministic run to run.
+#include "st3d_f16.cuh"
 #include "st3d_internal.h"
 
 namespace st3d {
@@ -44,7 +45,7 @@ struct BlobParams {
 
 template <typename T>
 __global__ void k_fill(Layout L, T* __restrict__ dst, int kind, uint64_t seed, unsigned field,
-                       double a, double b, BlobParams bp) {
+                       double a, double b, BlobParams bp, int interior_only) {
   // one thread per element of a row segment; grid.y over rows of all planes
   const long long row = blockIdx.y + (long long)gridDim.y * blockIdx.z;
   if (row >= (long long)L.nj * L.ni) return;
@@ -54,13 +55,16 @@ __global__ void k_fill(Layout L, T* __restrict__ dst, int kind, uint64_t seed, u
        kk += (long long)gridDim.x * blockDim.x) {
     const long long k = kk - L.pk;
     double val;
-    if (kind == ST3D_FILL_CONST) {
+    const bool inner = i >= 0 && i < L.xs && j >= 0 && j < L.ys && k >= 0 && k < L.zs;
+    if (interior_only && !inner) {
+      val = 0.0;
+    } else if (kind == ST3D_FILL_CONST) {
       val = a;
     } else if (kind == ST3D_FILL_UNIFORM) {
       val = a + (b - a) * unit_at(seed, field, i, j, k);
     } else {
       val = 0.0;
-      if (i >= 0 && i < L.xs && j >= 0 && j < L.ys && k >= 0 && k < L.zs) {
+      if (inner) {
         const double inv = 1.0 / (2.0 * b * b);
         for (int q = 0; q < bp.n; ++q) {
           const double di = (double)i - bp.p[4 * q], dj = (double)j - bp.p[4 * q + 1],
@@ -73,30 +77,42 @@ __global__ void k_fill(Layout L, T* __restrict__ dst, int kind, uint64_t seed, u
   }
 }
 
-template <typename T>
-__global__ void k_check(Geom g, const T* __restrict__ v, double expected, double tol,
+__device__ __forceinline__ double load_field(const FieldRef& f, long long i, long long x) {
+  switch (f.storage) {
+    case ST3D_F64: return static_cast<const double*>(f.p)[x];
+    case ST3D_F32: return (double)static_cast<const float*>(f.p)[x];
+    case ST3D_F16:
+    case ST3D_F16_HILO: {
+      const uint16_t w = static_cast<const uint16_t*>(f.p)[x];
+      float v = __half2float(__ushort_as_half(w));
+      if (f.lo) v = __fmaf_rn((float)f.lo[x], ulp256_f16(w), v);
+      return (double)(v * exp2i(f.E[i]));
+    }
+    case ST3D_BF16: {
+      const uint16_t w = static_cast<const uint16_t*>(f.p)[x];
+      return (double)(__uint_as_float((uint32_t)w << 16) * exp2i(f.E[i]));
+    }
+    default: return 0.0;
+  }
+}
+
+__global__ void k_check(Geom g, FieldRef v, double expected, double tol,
                         unsigned long long* counter) {
   unsigned long long local = 0;
   const long long nrows = (long long)g.xs * g.ys;
   for (long long r = blockIdx.x; r < nrows; r += gridDim.x) {
     const long long i = r / g.ys, j = r % g.ys;
-    const T* row = v + g.org + i * g.si + j * g.sj;
+    const long long row = g.org + i * g.si + j * g.sj;
     for (int k = threadIdx.x; k < g.zs; k += blockDim.x)
-      if (fabs((double)row[k] - expected) > tol) ++local;
+      if (fabs(load_field(v, i, row + k) - expected) > tol) ++local;
   }
   if (local) atomicAdd(counter, local);
 }
 
 constexpr int kNormThreads = 256;
 
-__device__ __forceinline__ double load_as_double(const void* p, int storage, long long x) {
-  if (storage == ST3D_F64) return static_cast<const double*>(p)[x];
-  return (double)static_cast<const float*>(p)[x];
-}
-
 __global__ void __launch_bounds__(kNormThreads)
-    k_norms_partial(int sa, Geom ga, const void* __restrict__ a, int sb, Geom gb,
-                    const void* __restrict__ b, double* __restrict__ partial) {
+    k_norms_partial(Geom ga, FieldRef a, Geom gb, FieldRef b, double* __restrict__ partial) {
   double d2 = 0.0, b2 = 0.0, dm = 0.0, bm = 0.0;
   const long long nrows = (long long)ga.xs * ga.ys;
   for (long long r = blockIdx.x; r < nrows; r += gridDim.x) {
@@ -104,8 +120,8 @@ __global__ void __launch_bounds__(kNormThreads)
     const long long xa = ga.org + i * ga.si + j * ga.sj;
     const long long xb = gb.org + i * gb.si + j * gb.sj;
     for (int k = threadIdx.x; k < ga.zs; k += blockDim.x) {
-      const double va = load_as_double(a, sa, xa + k);
-      const double vb = b ? load_as_double(b, sb, xb + k) : 0.0;
+      const double va = load_field(a, i, xa + k);
+      const double vb = b.p ? load_field(b, i, xb + k) : 0.0;
       const double d = va - vb;
       d2 += d * d;
       b2 += vb * vb;
@@ -159,7 +175,7 @@ __global__ void __launch_bounds__(kNormThreads)
 
 cudaError_t launch_fill(int storage, const Layout& L, void* dst, int kind, uint64_t seed,
                         unsigned field, double a, double b, const double* blob_params, int nblobs,
-                        cudaStream_t stream) {
+                        int interior_only, cudaStream_t stream) {
   BlobParams bp;
   bp.n = nblobs < 0 ? 0 : (nblobs > 16 ? 16 : nblobs);
   for (int q = 0; q < 4 * bp.n; ++q) bp.p[q] = blob_params[q];
@@ -170,23 +186,17 @@ cudaError_t launch_fill(int storage, const Layout& L, void* dst, int kind, uint6
   dim3 grid((L.nk + 255) / 256, gy, gz);
   const int k = kind;
   if (storage == ST3D_F32)
-    k_fill<float><<<grid, block, 0, stream>>>(L, (float*)dst, k, seed, field, a, b, bp);
+    k_fill<float><<<grid, block, 0, stream>>>(L, (float*)dst, k, seed, field, a, b, bp, interior_only);
   else if (storage == ST3D_F64)
-    k_fill<double><<<grid, block, 0, stream>>>(L, (double*)dst, k, seed, field, a, b, bp);
+    k_fill<double><<<grid, block, 0, stream>>>(L, (double*)dst, k, seed, field, a, b, bp, interior_only);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
-cudaError_t launch_check(int storage, const Geom& g, const void* v, double expected, double tol,
+cudaError_t launch_check(const Geom& g, const FieldRef& v, double expected, double tol,
                          unsigned long long* counter, cudaStream_t stream) {
-  const int blocks = 4 * 152;
-  if (storage == ST3D_F32)
-    k_check<float><<<blocks, 256, 0, stream>>>(g, (const float*)v, expected, tol, counter);
-  else if (storage == ST3D_F64)
-    k_check<double><<<blocks, 256, 0, stream>>>(g, (const double*)v, expected, tol, counter);
-  else
-    return cudaErrorInvalidValue;
+  k_check<<<4 * 152, 256, 0, stream>>>(g, v, expected, tol, counter);
   return cudaGetLastError();
 }
 
@@ -195,10 +205,9 @@ int norms_blocks(const Geom& g) {
   return (int)(rows < 8 * 152 ? rows : 8 * 152);
 }
 
-cudaError_t launch_norms(int sa, const Geom& ga, const void* a, int sb, const Geom& gb,
-                         const void* b, double* scratch, int nblocks, double* out_dev,
-                         cudaStream_t stream) {
-  k_norms_partial<<<nblocks, kNormThreads, 0, stream>>>(sa, ga, a, sb, gb, b, scratch);
+cudaError_t launch_norms(const Geom& ga, const FieldRef& a, const Geom& gb, const FieldRef& b,
+                         double* scratch, int nblocks, double* out_dev, cudaStream_t stream) {
+  k_norms_partial<<<nblocks, kNormThreads, 0, stream>>>(ga, a, gb, b, scratch);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_norms_final<<<1, kNormThreads, 0, stream>>>(scratch, nblocks, out_dev);

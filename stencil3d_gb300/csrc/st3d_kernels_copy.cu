@@ -79,3 +79,141 @@ cudaError_t launch_dev_to_ref(int eb, const Layout& L, const RefGeom& R, const v
 }
 
 }  // namespace st3d
+
+// ---------------------------------------------------------------------------
+// 16-bit storage (st3d_f16.cuh): host arrays stay float; the device keeps a
+// 16-bit word per point (plus a low byte in the compensated form) and a
+// power-of-two scale per i-plane.
+// ---------------------------------------------------------------------------
+#include "st3d_f16.cuh"
+
+namespace st3d {
+
+namespace {
+
+template <int KIND>
+__device__ __forceinline__ float word_to_float(uint16_t b) {
+  if (KIND == 0) return __half2float(__ushort_as_half(b));
+  return __uint_as_float((uint32_t)b << 16);
+}
+template <int KIND>
+__device__ __forceinline__ uint16_t float_to_word(float x) {
+  if (KIND == 0) return __half_as_ushort(__float2half_rn(x));
+  return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+
+// Per-plane maxima of |x| over the interior (float bits, atomicMax) and the
+// maximum over the halo points the stencil reads.
+__global__ void k_plane_max_ref(RefGeom R, const float* __restrict__ stage, uint32_t* __restrict__ M,
+                                uint32_t* __restrict__ halo_max, int hx, int hy, int hz) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = (int)blockIdx.y - hy;
+  const int i = (int)blockIdx.z - hx;
+  const int k = kk - hz;
+  float m_in = 0.0f, m_halo = 0.0f;
+  if (kk < R.zs + 2 * hz) {
+    const float x = fabsf(stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k]);
+    const bool inner = i >= 0 && i < R.xs && j >= 0 && j < R.ys && k >= 0 && k < R.zs;
+    if (inner) m_in = x; else m_halo = x;
+  }
+  const uint32_t a = __reduce_max_sync(0xffffffffu, __float_as_uint(m_in));
+  const uint32_t b = __reduce_max_sync(0xffffffffu, __float_as_uint(m_halo));
+  if ((threadIdx.x & 31) == 0) {
+    if (a && i >= 0 && i < R.xs) atomicMax(&M[i], a);
+    if (b) atomicMax(halo_max, b);
+  }
+}
+
+// Scatter + encode: staging (reference layout, float) -> words (+ low bytes)
+// in the library layout, the plane's scale from its maximum.
+template <int KIND, bool HILO>
+__global__ void k_ref_to_dev16(Layout L, RefGeom R, const float* __restrict__ stage,
+                               uint16_t* __restrict__ hi, int8_t* __restrict__ lo,
+                               const uint32_t* __restrict__ M, int* __restrict__ E, int hx, int hy,
+                               int hz) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= R.zs + 2 * hz) return;
+  const int j = (int)blockIdx.y - hy;
+  const int i = (int)blockIdx.z - hx;
+  const int k = kk - hz;
+  const bool plane_in = i >= 0 && i < R.xs;
+  const int e = plane_in ? scale_exponent(__uint_as_float(M[i])) : 0;
+  if (plane_in && kk == 0 && blockIdx.y == 0) E[i] = e;
+  const float xs = stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k] * exp2i(-e);
+  const long long d = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
+  const uint16_t w = float_to_word<KIND>(xs);
+  hi[d] = w;
+  if (HILO) {
+    const float r = xs - word_to_float<KIND>(w);
+    int eb = (w >> 10) & 0x1f;
+    if (eb == 0) eb = 1;
+    int q = __float2int_rn(r * exp2i(33 - eb));
+    q = q > 127 ? 127 : (q < -127 ? -127 : q);
+    lo[d] = (int8_t)q;
+  }
+}
+
+// Gather + decode: words (+ low bytes) -> staging (reference layout, float),
+// interior rows with their k halo.
+template <int KIND, bool HILO>
+__global__ void k_dev16_to_ref(Layout L, RefGeom R, const uint16_t* __restrict__ hi,
+                               const int8_t* __restrict__ lo, const int* __restrict__ E,
+                               float* __restrict__ stage, int hz) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= R.zs + 2 * hz) return;
+  const int j = (int)blockIdx.y;
+  const int i = (int)blockIdx.z;
+  const int k = kk - hz;
+  const long long s = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
+  const uint16_t w = hi[s];
+  float x = word_to_float<KIND>(w);
+  if (HILO) x = __fmaf_rn((float)lo[s], ulp256_f16(w), x);
+  stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k] = x * exp2i(E[i]);
+}
+
+}  // namespace
+
+cudaError_t launch_plane_max_ref(const RefGeom& R, const float* stage, uint32_t* M,
+                                 uint32_t* halo_max, int hx, int hy, int hz, cudaStream_t stream) {
+  dim3 block(256);
+  dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys + 2 * hy, R.xs + 2 * hx);
+  if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
+  k_plane_max_ref<<<grid, block, 0, stream>>>(R, stage, M, halo_max, hx, hy, hz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ref_to_dev16(int storage, const Layout& L, const RefGeom& R, const float* stage,
+                                uint16_t* hi, int8_t* lo, const uint32_t* M, int* E, int hx, int hy,
+                                int hz, cudaStream_t stream) {
+  dim3 block(256);
+  dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys + 2 * hy, R.xs + 2 * hx);
+  if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
+  if (storage == ST3D_F16)
+    k_ref_to_dev16<0, false><<<grid, block, 0, stream>>>(L, R, stage, hi, lo, M, E, hx, hy, hz);
+  else if (storage == ST3D_BF16)
+    k_ref_to_dev16<1, false><<<grid, block, 0, stream>>>(L, R, stage, hi, lo, M, E, hx, hy, hz);
+  else if (storage == ST3D_F16_HILO)
+    k_ref_to_dev16<0, true><<<grid, block, 0, stream>>>(L, R, stage, hi, lo, M, E, hx, hy, hz);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dev16_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* hi,
+                                const int8_t* lo, const int* E, float* stage, int hz,
+                                cudaStream_t stream) {
+  dim3 block(256);
+  dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys, R.xs);
+  if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
+  if (storage == ST3D_F16)
+    k_dev16_to_ref<0, false><<<grid, block, 0, stream>>>(L, R, hi, lo, E, stage, hz);
+  else if (storage == ST3D_BF16)
+    k_dev16_to_ref<1, false><<<grid, block, 0, stream>>>(L, R, hi, lo, E, stage, hz);
+  else if (storage == ST3D_F16_HILO)
+    k_dev16_to_ref<0, true><<<grid, block, 0, stream>>>(L, R, hi, lo, E, stage, hz);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+}  // namespace st3d

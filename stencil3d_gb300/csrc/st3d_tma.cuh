@@ -28,6 +28,21 @@ struct TmaPlan {
   CUtensorMap vmap[3];  // interior box (kTmaTK x tj x 1) over each field buffer
 };
 
+// Plan of the 16-bit-storage kernel (st3d_kernels_tma16.cu): same work
+// decomposition; tensor maps over the 16-bit words of the u/v buffers (halo
+// box and interior box), of s (interior box, index 2), and over the low
+// bytes of the u/v buffers.
+struct Tma16Plan {
+  int tj = 16, nv = 3, ichunk = 128, radius = 0;
+  int ntj = 0, ntk = 0, nti = 0, units = 0;
+  int grid = 0, threads = 0;
+  size_t smem = 0;
+  uint64_t timeout_ns = 4000000000ull;
+  CUtensorMap uhi[2];
+  CUtensorMap vhi[3];
+  CUtensorMap lo[2];
+};
+
 // Planes per work unit: the chunk length that minimises the modelled time
 // ceil(units / ctas) * (ichunk + R/2) (a unit's 2R warm-up steps load only u,
 // about a quarter of a full step's bytes), i.e. balance across the persistent

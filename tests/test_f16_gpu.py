@@ -1,0 +1,94 @@
+"""GPU parity of the precision form: FP16 / BF16 words with a power-of-two
+scale per i-plane, and FP16 + a compensating byte, all arithmetic in FP32.
+
+The library's 16-bit kernels and the oracle's restatement of the same
+encoding, scale rule and update must agree bit for bit (decoded u and v
+after several steps), for the 7-, 13- and 25-point stencils.  The 16-bit
+forms keep a zero halo (a zero Dirichlet boundary); other halos are refused.
+"""
+import numpy as np
+import pytest
+
+import stencil3d_gb300 as S
+from oracle import oracle as O
+from tests.helpers import halo_mask, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(grid, seed, blobs):
+    if blobs:
+        u = O.fill_blobs(grid, seed, 4, 6.0)
+    else:
+        u = O.fill_uniform(grid, seed, 0, -1e-3, 1e-3)
+        u[halo_mask(grid)] = 0.0
+    v = u * np.float32(0.999) if blobs else O.fill_uniform(grid, seed, 1, -1e-3, 1e-3)
+    v[halo_mask(grid)] = 0.0
+    s = np.zeros_like(u)
+    return np.ascontiguousarray(v), s, u
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_hilo"])
+@pytest.mark.parametrize("points", [7, 13, 25])
+@pytest.mark.parametrize("grid,blobs", [((24, 40, 150, 4, 4, 4), True),
+                                        ((9, 17, 64, 4, 4, 16), False)])
+def test_f16_forms_match_oracle(storage, points, grid, blobs):
+    dt = 1e-3 if points == 7 else 5e-4
+    steps = 9
+    src = (grid[0] // 2, grid[1] // 2, grid[2] // 2)
+    v, s, u = _inputs(grid, 3 + points, blobs)
+    g = S.Grid(*grid)
+    with S.Stencil(g, points, "wave", storage, dt=dt, src=src) as st:
+        assert st.info().kernel == S.KERNEL_TMA
+        uu, vv = u.copy(), v.copy()
+        st.iterate_host(vv, s, uu, steps)
+    kind, hilo = O.storage_kind(storage)
+    c0, c1, c2 = O.wave_constants(points, 1500.0, dt, 10.0)
+    fu, fv, fs = (O.Field16(x, grid, kind, hilo) for x in (u, v, s))
+    O.iterate_wave16(fu, fv, fs, grid, points, steps, np.float32(c1), np.float32(c2), src=src,
+                     amps=O.ricker_amps(0, steps, dt))
+    np.testing.assert_array_equal(O.interior(uu, grid), O.interior(fu.decode(), grid))
+    np.testing.assert_array_equal(O.interior(vv, grid), O.interior(fv.decode(), grid))
+
+
+@pytest.mark.parametrize("storage,bound", [("f16_hilo", 3e-4), ("f16", 1e-1), ("bf16", 1.0)])
+def test_f16_forms_track_fp64(storage, bound):
+    """Accuracy of each form against FP64 after 60 steps of a smooth field."""
+    grid = (32, 36, 140, 4, 4, 4)
+    dt = 5e-4
+    v, s, u = _inputs(grid, 11, True)
+    g = S.Grid(*grid)
+    with S.Stencil(g, 25, "wave", storage, dt=dt) as a, S.Stencil(g, 25, "wave", "f64", dt=dt) as b:
+        a.upload(v, s, u)
+        b.upload(v.astype(np.float64), s.astype(np.float64), u.astype(np.float64))
+        a.iterate(60)
+        b.iterate(60)
+        a.synchronize()
+        b.synchronize()
+        err = a.rel_l2(b)
+    assert err < bound, err
+
+
+def test_f16_rejects_nonzero_halo():
+    grid = (8, 20, 40, 4, 4, 4)
+    u = O.fill_uniform(grid, 1, 0, -1.0, 1.0)
+    g = S.Grid(*grid)
+    with S.Stencil(g, 7, "wave", "f16") as st:
+        with pytest.raises(S.St3dError) as e:
+            st.upload(u=u)
+        assert e.value.status == S.api.ERR_UNSUPPORTED
+
+
+def test_f16_norms_and_fill():
+    grid = (12, 20, 70, 4, 4, 4)
+    g = S.Grid(*grid)
+    with S.Stencil(g, 13, "wave", "f16_hilo", dt=5e-4) as st:
+        st.fill(S.FIELD_U, S.FILL_BLOBS, 5, 3, 4.0)
+        st.fill(S.FIELD_V, S.FILL_CONST, 0, 0.0)
+        st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
+        u = g.empty()
+        st.download(u=u)
+        e2, _, em, _ = st.norms(S.FIELD_U)
+        ui = g.interior(u).astype(np.float64)
+        assert np.isclose(e2, np.sum(ui ** 2), rtol=1e-12) and em == np.max(np.abs(ui))
+        assert np.all(u[halo_mask(grid)] == 0.0)
