@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target CPU time of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--batch-steps", type=int, default=500,
+                   help="steps of the batching-form run: 64 seeded grids (0 to skip)")
     p.add_argument("--precision-forms", default="f16_hilo,f16,bf16",
                    help="16-bit storage forms timed and judged against FP64 ('' to skip)")
     return p.parse_args()
@@ -189,6 +191,54 @@ def accuracy_run(S, wl, steps, kernel, storages):
         r.close()
     ref.close()
     return report
+
+
+def batch_specs(seed=SEED, n=64):
+    """The batching workload: n grids, each axis uniform in 64..320 cells,
+    stencil order from {7, 13, 25}, a Ricker source at a random interior
+    point, FP32 wave form (seeded)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n):
+        xs, ys, zs = (int(x) for x in rng.integers(64, 321, size=3))
+        pts = int(rng.choice([7, 13, 25]))
+        src = tuple(int(rng.integers(0, d)) for d in (xs, ys, zs))
+        specs.append(((xs, ys, zs), pts, src))
+    return specs
+
+
+def batch_run(S, steps, warmup):
+    """Aggregate throughput of the batching form under each schedule."""
+    specs = batch_specs()
+    grids = [S.Grid(xs, ys, zs, 4, 4, 4) for (xs, ys, zs), _, _ in specs]
+    pts = [p for _, p, _ in specs]
+    dts = [1e-3 if p == 7 else 5e-4 for p in pts]
+    srcs = [s for _, _, s in specs]
+    out = {"grids": len(specs), "steps": steps,
+           "workload": "64 grids, axes U{64..320}, orders {7,13,25}, FP32 wave, seeded sources"}
+    with S.Batch(grids, pts, dt=dts, srcs=srcs) as b:
+        for i in range(len(grids)):
+            st = b.context(i)
+            st.fill(S.FIELD_U, S.FILL_BLOBS, SEED + i, 4, 12.0)
+            st.fill(S.FIELD_V, S.FILL_BLOBS, SEED + i, 4, 12.0)
+            st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
+        info = b.info()
+        total = info.interior_points
+        out["points"] = int(total)
+        out["work_items_per_step"] = int(info.work_items)
+        for schedule in ("sequential", "persistent", "graph"):
+            b.iterate(warmup, schedule)
+            b.synchronize()
+            l0 = b.info().launches
+            b.timer_start()
+            b.iterate(steps, schedule)
+            ms = b.timer_stop()
+            b.synchronize()
+            out[schedule] = {"value": total * steps / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+                             "ms_per_step": ms / steps,
+                             "launches": int(b.info().launches - l0)}
+    out["graph_vs_sequential"] = out["graph"]["value"] / out["sequential"]["value"]
+    return out
 
 
 def time_storage(S, wl, storage, steps, warmup, kernel="auto"):
@@ -354,6 +404,9 @@ def run_gb300(args, dist):
         for form in forms:
             result["fp16"][form]["accuracy_vs_fp64"] = acc[form]
             result["fp16"][form]["l2_err_vs_fp64"] = acc[form][-1]["rel_l2"]
+
+    if dist.rank == 0 and args.batch_steps > 0:
+        result["batch"] = batch_run(S, args.batch_steps, args.warmup)
 
     host = None
     if args.e2e_calls > 0:

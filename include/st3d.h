@@ -110,7 +110,8 @@ typedef struct st3d_opts {
   int32_t temporal_block;            /* mode W steps fused per pass: 1, 2 or 4 */
   int32_t tile_j, tile_k;            /* CTA tile; 0 = automatic */
   int32_t ichunk;                    /* planes per work unit along i; 0 = automatic */
-  int32_t reserved[8];
+  int32_t stages;                    /* pipeline stages of the TMA kernels; 0 = automatic */
+  int32_t reserved[7];
 } st3d_opts;
 
 typedef struct st3d_info {
@@ -225,6 +226,49 @@ int st3d_host_free(void* ptr);
 /* The Ricker wavelet the mode W source uses: (1 - 2a) exp(-a),
  * a = (pi f (t - t0))^2, evaluated on the host in double. */
 double st3d_ricker(double t, double f, double t0);
+
+/* ---- batching form --------------------------------------------------------
+ * No counterpart in the reference, which advances one grid per process:
+ * many independent grids of uneven sizes and stencil orders (independent
+ * source shots) advance together.  Every grid is a context of the FP32 wave
+ * form (7, 13 or 25 points) living on the batch's stream; per-grid upload,
+ * download, fill and norms go through st3d_batch_context.  Schedules of one
+ * call of st3d_batch_iterate:
+ *   ST3D_BATCH_SEQUENTIAL  one single-grid launch per grid per step;
+ *   ST3D_BATCH_PERSISTENT  one persistent launch per step whose CTAs pull
+ *                          (grid, tile, chunk) items from a device work queue;
+ *   ST3D_BATCH_GRAPH       the persistent schedule with the whole time loop
+ *                          captured once in a CUDA graph (cached by step
+ *                          count) and replayed. */
+typedef struct st3d_batch st3d_batch;
+
+typedef enum st3d_batch_schedule {
+  ST3D_BATCH_SEQUENTIAL = 0,
+  ST3D_BATCH_PERSISTENT = 1,
+  ST3D_BATCH_GRAPH = 2
+} st3d_batch_schedule;
+
+typedef struct st3d_batch_info {
+  uint32_t grids;           /* grids in the batch */
+  uint32_t work_items;      /* queue items per step: one per (grid, tile, i-chunk) */
+  uint32_t ctas;            /* persistent CTAs per launch */
+  uint32_t graphs;          /* captured time loops */
+  uint64_t interior_points; /* sum of xs*ys*zs over the grids */
+  uint64_t launches;        /* kernel launches issued by st3d_batch_iterate */
+  int32_t reserved[8];
+} st3d_batch_info;
+
+int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* opts,
+                      st3d_batch** batch);
+int st3d_batch_destroy(st3d_batch* batch);
+/* The context of grid idx (owned by the batch: do not destroy it). */
+int st3d_batch_context(st3d_batch* batch, uint32_t idx, st3d_ctx** ctx);
+int st3d_batch_get_info(const st3d_batch* batch, st3d_batch_info* info);
+/* Advance every grid `steps` leapfrog steps with the given schedule. */
+int st3d_batch_iterate(st3d_batch* batch, uint32_t steps, int schedule);
+int st3d_batch_synchronize(st3d_batch* batch);
+int st3d_batch_timer_start(st3d_batch* batch);
+int st3d_batch_timer_stop(st3d_batch* batch, float* ms);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -48,7 +48,7 @@ class Opts(C.Structure):
                 ("pad0", C.c_int32),
                 ("src_f", C.c_double), ("src_t0", C.c_double), ("dt", C.c_double),
                 ("temporal_block", C.c_int32), ("tile_j", C.c_int32), ("tile_k", C.c_int32),
-                ("ichunk", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("ichunk", C.c_int32), ("stages", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class Info(C.Structure):
@@ -61,6 +61,15 @@ class Info(C.Structure):
                 ("tile_j", C.c_int32), ("tile_k", C.c_int32), ("ichunk", C.c_int32),
                 ("temporal_block", C.c_int32), ("reserved", C.c_int32 * 8)]
 
+
+class BatchInfo(C.Structure):
+    _fields_ = [("grids", C.c_uint32), ("work_items", C.c_uint32), ("ctas", C.c_uint32),
+                ("graphs", C.c_uint32), ("interior_points", C.c_uint64), ("launches", C.c_uint64),
+                ("reserved", C.c_int32 * 8)]
+
+
+BATCH_SEQUENTIAL, BATCH_PERSISTENT, BATCH_GRAPH = 0, 1, 2
+_SCHEDULES = {"sequential": BATCH_SEQUENTIAL, "persistent": BATCH_PERSISTENT, "graph": BATCH_GRAPH}
 
 _lib = None
 
@@ -100,6 +109,14 @@ def lib():
             "st3d_host_free": ([vp], i),
             "st3d_ricker": ([C.c_double, C.c_double, C.c_double], C.c_double),
             "st3d_norms_noalloc": ([C.POINTER(GridDesc), vp, i, vp, i, vp, vp], i),
+            "st3d_batch_create": ([C.c_uint32, C.POINTER(GridDesc), C.POINTER(Opts), C.POINTER(vp)], i),
+            "st3d_batch_destroy": ([vp], i),
+            "st3d_batch_context": ([vp, C.c_uint32, C.POINTER(vp)], i),
+            "st3d_batch_get_info": ([vp, C.POINTER(BatchInfo)], i),
+            "st3d_batch_iterate": ([vp, C.c_uint32, i], i),
+            "st3d_batch_synchronize": ([vp], i),
+            "st3d_batch_timer_start": ([vp], i),
+            "st3d_batch_timer_stop": ([vp, C.POINTER(C.c_float)], i),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -222,17 +239,22 @@ class Stencil:
     numpy arrays in and out; ``iterate(n)`` advances n steps on the device.
     """
 
-    def __init__(self, grid, points=7, mode="ref", storage="f32", opts=None, **kw):
+    def __init__(self, grid, points=7, mode="ref", storage="f32", opts=None, _handle=None, **kw):
         self.grid = grid
         self.opts = opts if opts is not None else default_opts(points, mode, storage, **kw)
         self.dtype = np.float64 if self.opts.storage == F64 else np.float32
-        h = C.c_void_p()
-        _ck(lib().st3d_create(C.byref(grid.desc()), C.byref(self.opts), C.byref(h)))
-        self._h = h
+        self._owned = _handle is None
+        if _handle is None:
+            h = C.c_void_p()
+            _ck(lib().st3d_create(C.byref(grid.desc()), C.byref(self.opts), C.byref(h)))
+            self._h = h
+        else:
+            self._h = _handle
 
     def close(self):
         if getattr(self, "_h", None):
-            lib().st3d_destroy(self._h)
+            if self._owned:
+                lib().st3d_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -297,6 +319,79 @@ class Stencil:
         ms = C.c_float()
         _ck(lib().st3d_timer_stop(self._h, C.byref(ms)))
         return ms.value
+
+
+class Batch:
+    """Many independent grids (FP32 wave form, 7/13/25 points) advancing
+    together: ``Batch(grids, points, dt=..., srcs=...)``; ``context(i)`` is a
+    Stencil view of grid i for upload/download/fill/norms; ``iterate(n,
+    schedule)`` with schedule "sequential", "persistent" or "graph"."""
+
+    def __init__(self, grids, points, dt=None, srcs=None, **kw):
+        n = len(grids)
+        self.grids = list(grids)
+        descs = (GridDesc * n)(*[g.desc() for g in grids])
+        opts = (Opts * n)()
+        for i, (g, p) in enumerate(zip(grids, points)):
+            extra = dict(kw)
+            if dt is not None:
+                extra["dt"] = dt[i] if isinstance(dt, (list, tuple)) else dt
+            if srcs is not None:
+                extra["src"] = srcs[i]
+            opts[i] = default_opts(p, "wave", "f32", **extra)
+        self.opts = opts
+        h = C.c_void_p()
+        _ck(lib().st3d_batch_create(n, descs, opts, C.byref(h)))
+        self._h = h
+        self._views = []
+        for i in range(n):
+            c = C.c_void_p()
+            _ck(lib().st3d_batch_context(self._h, i, C.byref(c)))
+            self._views.append(Stencil(grids[i], opts=opts[i], _handle=c))
+
+    def context(self, i):
+        return self._views[i]
+
+    def __len__(self):
+        return len(self._views)
+
+    def iterate(self, steps, schedule="graph"):
+        _ck(lib().st3d_batch_iterate(self._h, int(steps), _SCHEDULES.get(schedule, schedule)))
+
+    def synchronize(self):
+        _ck(lib().st3d_batch_synchronize(self._h))
+
+    def info(self):
+        info = BatchInfo()
+        _ck(lib().st3d_batch_get_info(self._h, C.byref(info)))
+        return info
+
+    def timer_start(self):
+        _ck(lib().st3d_batch_timer_start(self._h))
+
+    def timer_stop(self):
+        ms = C.c_float()
+        _ck(lib().st3d_batch_timer_stop(self._h, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            for v in self._views:
+                v.close()
+            lib().st3d_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class PinnedArray:

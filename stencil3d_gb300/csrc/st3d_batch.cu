@@ -1,0 +1,630 @@
+// st3d_batch.cu -- the batching form: many independent grids of uneven
+// sizes and stencil orders (independent source shots) advancing together.
+//
+// One time step of every grid is one persistent launch: CTAs (at most
+// #SMs x resident) pull work items -- one (grid, 16-row x 128-point tile,
+// i-chunk) unit each -- from a device work queue (an atomic head over an item
+// table ordered largest grid first), so small and large grids, 7-, 13- and
+// 25-point stencils share the GPU without a launch per grid.  The producer
+// warp of each CTA takes the next item, streams that grid's planes in with
+// TMA (the grid's own tensor maps, kept in global memory) and tells the
+// consumer warps which item each pipeline stage belongs to; the consumers run
+// the stencil of the item's order (the same code and arithmetic as the
+// single-grid TMA kernel).  Steps are ordered by kernel boundaries; the whole
+// time loop (a queue reset and a launch per step) can be captured in a CUDA
+// graph and replayed.  The baseline schedule launches the single-grid kernel
+// once per grid per step.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "st3d_ctx.h"
+#include "st3d_internal.h"
+#include "st3d_tma.cuh"
+
+namespace st3d {
+
+namespace {
+
+constexpr int kBTJ = 16;
+constexpr int kBNV = 3;
+constexpr int kBRmax = 4;
+
+struct BatchGrid {
+  Geom g;
+  Coefs<float> cf;
+  float* buf[2];
+  int P, R;
+  int ntk, ntjk, ichunk, units;
+  int src_i, src_j, src_k;
+  int cur0;      // buffer holding u at the call's first step
+  int map_base;  // index of the grid's 5 tensor maps: u over buf 0/1, v over buf 0/1, s
+};
+
+struct BatchArgs {
+  const BatchGrid* grids;
+  const CUtensorMap* maps;
+  const int2* items;  // (grid, unit)
+  int total_items;
+  int n_grids;
+  int* head;
+  const float* amps;  // [step][grid]
+  int step;           // step within the call
+  uint64_t timeout_ns;
+  uint32_t* status;
+};
+
+struct BStage {
+  int grid;  // -1: no more work
+  int unit;
+  int pad[2];
+};
+
+constexpr int kUSlot = (kTmaUKW * (kBTJ + 2 * kBRmax) + 31) / 32 * 32;  // floats
+constexpr int kVSlot = kTmaTK * kBTJ;                                   // floats
+constexpr int kNU = kBNV + kBRmax;
+
+size_t batch_smem_bytes() {
+  return ((size_t)kNU * kUSlot + 2 * (size_t)kBNV * kVSlot) * 4 + 2 * kBNV * 8 + kBNV * sizeof(BStage) + 128;
+}
+
+// The consumer side of one work unit (the single-grid kernel's consumer loop
+// for stencil P): nsteps pipeline stages starting at global stage h0.
+template <int P>
+__device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid& G, int gi, int unit,
+                                             uint32_t h0, float* ur, float* vr, float* sr,
+                                             uint64_t* full, uint64_t* empty, int r, int lane) {
+  constexpr int R = (P == 25) ? 4 : (P == 13) ? 2 : 1;
+  constexpr int QN = 2 * R + 1;
+  constexpr int NP = npairs_of(P);
+  constexpr int TK = kTmaTK;
+  constexpr int UKW = kTmaUKW;
+  const Geom& g = G.g;
+  const int ic = unit / G.ntjk;
+  const int rem = unit - ic * G.ntjk;
+  const int jt = rem / G.ntk;
+  const int kt = rem - jt * G.ntk;
+  const int j = jt * kBTJ + r;
+  const int k = kt * TK + 4 * lane;
+  const int ia = ic * G.ichunk;
+  const int ib = min(ia + G.ichunk, g.xs);
+  const int nsteps = (ib - ia) + 2 * R;
+  const bool row_ok = j < g.ys;
+  const int ub = G.cur0 ^ (a.step & 1);
+  float* vout = G.buf[ub ^ 1];
+  float* vrow = vout + g.org + (long long)j * g.sj + k;
+  const float amp = (G.src_i >= 0) ? a.amps[(size_t)a.step * a.n_grids + gi] : 0.0f;
+  float4 q[QN];
+  for (int n0 = 0; n0 < nsteps; n0 += QN) {
+#pragma unroll
+    for (int ph = 0; ph < QN; ++ph) {
+      const int n = n0 + ph;
+      if (n >= nsteps) break;
+      const uint32_t hh = h0 + (uint32_t)n;
+      const int stage = (int)(hh % kBNV);
+      if (!mbar_wait_bounded(&full[stage], (hh / kBNV) & 1u, a.timeout_ns)) {
+        atomicExch(a.status, (uint32_t)kDevTimeoutFull);
+        return false;
+      }
+      q[ph] = *reinterpret_cast<const float4*>(ur + (hh % kNU) * kUSlot + (r + R) * UKW + kTmaKHalo + 4 * lane);
+      if (n >= 2 * R) {
+        const int i = ia + n - 2 * R;
+        const float* uc = ur + ((hh - R) % kNU) * kUSlot + (r + R) * UKW;
+        const float4 c4 = q[(ph + QN - R) % QN];
+        const float4 l4 = *reinterpret_cast<const float4*>(uc + 4 * lane);
+        const float4 r4 = *reinterpret_cast<const float4*>(uc + 2 * kTmaKHalo + 4 * lane);
+        const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w, r4.x, r4.y, r4.z, r4.w};
+        float acc[4];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const int ax = pair_axis(P, p);
+          const int rr = pair_r(P, p);
+          float av[4], bv[4];
+          if (ax == 2) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              av[c] = w[4 + c - rr];
+              bv[c] = w[4 + c + rr];
+            }
+          } else if (ax == 1) {
+            const float4 A = *reinterpret_cast<const float4*>(uc - rr * UKW + kTmaKHalo + 4 * lane);
+            const float4 B = *reinterpret_cast<const float4*>(uc + rr * UKW + kTmaKHalo + 4 * lane);
+            av[0] = A.x; av[1] = A.y; av[2] = A.z; av[3] = A.w;
+            bv[0] = B.x; bv[1] = B.y; bv[2] = B.z; bv[3] = B.w;
+          } else {
+            const float4 A = q[(ph + 2 * QN - R - rr) % QN];
+            const float4 B = q[(ph + QN - R + rr) % QN];
+            av[0] = A.x; av[1] = A.y; av[2] = A.z; av[3] = A.w;
+            bv[0] = B.x; bv[1] = B.y; bv[2] = B.z; bv[3] = B.w;
+          }
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const float d = (av[c] + bv[c]) - (w[4 + c] + w[4 + c]);
+            acc[c] = p == 0 ? G.cf.cf[0] * d : __fmaf_rn(G.cf.cf[p], d, acc[c]);
+          }
+        }
+        const float4 v4 = *reinterpret_cast<const float4*>(vr + stage * kVSlot + r * TK + 4 * lane);
+        const float4 s4 = *reinterpret_cast<const float4*>(sr + stage * kVSlot + r * TK + 4 * lane);
+        const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+        float ss[4] = {s4.x, s4.y, s4.z, s4.w};
+        float o[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          if (i == G.src_i && j == G.src_j && k + c == G.src_k) ss[c] = ss[c] + amp;
+          float t = (w[4 + c] + w[4 + c]) - vv[c];
+          t = __fmaf_rn(G.cf.c1, acc[c], t);
+          o[c] = __fmaf_rn(G.cf.c2, ss[c], t);
+        }
+        if (row_ok) {
+          float* dst = vrow + (long long)i * g.si;
+          if (k + 3 < g.zs) {
+            *reinterpret_cast<float4*>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+              if (k + c < g.zs) dst[c] = o[c];
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[stage]);
+    }
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* ur = reinterpret_cast<float*>(smem_raw);
+  float* vr = ur + kNU * kUSlot;
+  float* sr = vr + kBNV * kVSlot;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sr + kBNV * kVSlot);
+  uint64_t* empty = full + kBNV;
+  BStage* info = reinterpret_cast<BStage*>(empty + kBNV);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kBNV; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kBTJ);
+    }
+    fence_barrier_init();
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
+
+  if (warp == kBTJ) {
+    // ---------------- producer ----------------
+    if (lane != 0) return;
+    uint32_t h = 0;
+    bool ok = true;
+    while (ok) {
+      const int item = atomicAdd(a.head, 1);
+      const bool stop = item >= a.total_items;
+      const int stage0 = (int)(h % kBNV);
+      if (stop) {
+        // hand the consumers a stop record through the pipeline
+        if (h >= (uint32_t)kBNV &&
+            !mbar_wait_bounded(&empty[stage0], ((h / kBNV) - 1) & 1u, a.timeout_ns)) {
+          atomicExch(a.status, (uint32_t)kDevTimeoutEmpty);
+          break;
+        }
+        info[stage0].grid = -1;
+        mbar_arrive(&full[stage0]);
+        break;
+      }
+      const int2 it = a.items[item];
+      const BatchGrid& G = a.grids[it.x];
+      const int R = G.R;
+      const int unit = it.y;
+      const int ic = unit / G.ntjk;
+      const int rem = unit - ic * G.ntjk;
+      const int jt = rem / G.ntk;
+      const int kt = rem - jt * G.ntk;
+      const int k0 = kt * kTmaTK, j0 = jt * kBTJ;
+      const int ia = ic * G.ichunk;
+      const int ib = min(ia + G.ichunk, G.g.xs);
+      const int nsteps = (ib - ia) + 2 * R;
+      const int ub = G.cur0 ^ (a.step & 1);
+      const CUtensorMap* umap = &a.maps[G.map_base + ub];
+      const CUtensorMap* vmap = &a.maps[G.map_base + 2 + (ub ^ 1)];
+      const CUtensorMap* smap = &a.maps[G.map_base + 4];
+      const uint32_t ubytes = (uint32_t)(kTmaUKW * (kBTJ + 2 * R) * 4);
+      const uint32_t vbytes = (uint32_t)(kVSlot * 4);
+      for (int n = 0; n < nsteps; ++n, ++h) {
+        const int stage = (int)(h % kBNV);
+        if (h >= (uint32_t)kBNV &&
+            !mbar_wait_bounded(&empty[stage], ((h / kBNV) - 1) & 1u, a.timeout_ns)) {
+          atomicExch(a.status, (uint32_t)kDevTimeoutEmpty);
+          ok = false;
+          break;
+        }
+        info[stage].grid = it.x;
+        info[stage].unit = unit;
+        const bool has_vs = n >= 2 * R;
+        mbar_arrive_expect_tx(&full[stage], ubytes + (has_vs ? 2 * vbytes : 0u));
+        tma_load_3d(ur + (h % kNU) * kUSlot, umap, &full[stage], G.g.pk + k0 - kTmaKHalo,
+                    G.g.pj + j0 - R, G.g.pi + ia - R + n);
+        if (has_vs) {
+          const int i = ia + n - 2 * R;
+          tma_load_3d(vr + stage * kVSlot, vmap, &full[stage], G.g.pk + k0, G.g.pj + j0, G.g.pi + i);
+          tma_load_3d(sr + stage * kVSlot, smap, &full[stage], G.g.pk + k0, G.g.pj + j0, G.g.pi + i);
+        }
+      }
+    }
+    // leave no copy in flight: wait until the last real stages were consumed
+    for (uint32_t m = (h > (uint32_t)kBNV ? h - kBNV : 0u); m < h; ++m)
+      (void)mbar_wait_bounded(&empty[m % kBNV], (m / kBNV) & 1u, a.timeout_ns);
+    return;
+  }
+
+  // ---------------- consumers ----------------
+  uint32_t h = 0;
+  while (true) {
+    const int stage = (int)(h % kBNV);
+    if (!mbar_wait_bounded(&full[stage], (h / kBNV) & 1u, a.timeout_ns)) {
+      atomicExch(a.status, (uint32_t)kDevTimeoutFull);
+      return;
+    }
+    const BStage st = info[stage];
+    if (st.grid < 0) return;
+    const BatchGrid& G = a.grids[st.grid];
+    bool ok;
+    int nsteps;
+    {
+      const int ic = st.unit / G.ntjk;
+      const int ia = ic * G.ichunk;
+      nsteps = (min(ia + G.ichunk, G.g.xs) - ia) + 2 * G.R;
+    }
+    switch (G.P) {
+      case 7: ok = consume_unit<7>(a, G, st.grid, st.unit, h, ur, vr, sr, full, empty, warp, lane); break;
+      case 13: ok = consume_unit<13>(a, G, st.grid, st.unit, h, ur, vr, sr, full, empty, warp, lane); break;
+      default: ok = consume_unit<25>(a, G, st.grid, st.unit, h, ur, vr, sr, full, empty, warp, lane); break;
+    }
+    if (!ok) return;
+    h += (uint32_t)nsteps;
+  }
+}
+
+}  // namespace
+}  // namespace st3d
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+using namespace st3d;
+
+struct st3d_batch {
+  std::vector<st3d_ctx*> ctx;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  BatchGrid* d_grids = nullptr;
+  CUtensorMap* d_maps = nullptr;
+  int2* d_items = nullptr;
+  int* d_head = nullptr;  // one queue head per step of the largest call
+  int heads = 0;
+  float* d_amps = nullptr;
+  size_t amps_cap = 0;
+  float* h_amps = nullptr;  // pinned staging of the amplitudes
+  cudaEvent_t amps_copied = nullptr;  // the last copy out of h_amps has been done
+  uint32_t* d_status = nullptr;
+  std::vector<BatchGrid> grids;
+  int total_items = 0;
+  int ctas = 0;
+  size_t smem = 0;
+  uint64_t launches = 0;
+  uint64_t points = 0;
+  std::map<uint32_t, cudaGraphExec_t> graphs;  // by step count
+};
+
+namespace {
+
+int bfail(int status, const char* msg) { return set_error(status, "%s", msg); }
+
+#define B_CUDA(call)                                                                            \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return set_error(e_ == cudaErrorMemoryAllocation ? ST3D_ERR_NOMEM : ST3D_ERR_CUDA,        \
+                       "%s: %s", #call, cudaGetErrorString(e_));                                \
+  } while (0)
+
+void destroy_graphs(st3d_batch* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+int ensure_steps(st3d_batch* b, uint32_t steps) {
+  const size_t need = (size_t)steps * b->ctx.size();
+  if (need > b->amps_cap) {
+    if (b->d_amps) cudaFree(b->d_amps);
+    if (b->h_amps) cudaFreeHost(b->h_amps);
+    b->d_amps = nullptr;
+    b->h_amps = nullptr;
+    B_CUDA(cudaMalloc(&b->d_amps, need * sizeof(float)));
+    B_CUDA(cudaMallocHost(&b->h_amps, need * sizeof(float)));
+    b->amps_cap = need;
+    destroy_graphs(b);  // captured launches point at the old buffer
+  }
+  if ((int)steps > b->heads) {
+    if (b->d_head) cudaFree(b->d_head);
+    b->d_head = nullptr;
+    B_CUDA(cudaMalloc(&b->d_head, (size_t)steps * sizeof(int)));
+    b->heads = (int)steps;
+    destroy_graphs(b);
+  }
+  return ST3D_OK;
+}
+
+// The per-call state the kernels read: the buffer holding u in each grid and
+// the source amplitudes of every step.
+int stage_call(st3d_batch* b, uint32_t steps) {
+  const size_t n = b->ctx.size();
+  // the previous call's asynchronous copy may still be reading h_amps
+  B_CUDA(cudaEventSynchronize(b->amps_copied));
+  for (size_t gi = 0; gi < n; ++gi) {
+    st3d_ctx* c = b->ctx[gi];
+    b->grids[gi].cur0 = c->cur;
+    for (uint32_t t = 0; t < steps; ++t) {
+      float amp = 0.0f;
+      if (c->opts.src_i >= 0)
+        amp = (float)st3d_ricker((double)(c->step + t) * c->opts.dt, c->opts.src_f, c->opts.src_t0);
+      b->h_amps[(size_t)t * n + gi] = amp;
+    }
+  }
+  B_CUDA(cudaMemcpyAsync(b->d_grids, b->grids.data(), n * sizeof(BatchGrid), cudaMemcpyHostToDevice,
+                         b->stream));
+  B_CUDA(cudaMemcpyAsync(b->d_amps, b->h_amps, (size_t)steps * n * sizeof(float),
+                         cudaMemcpyHostToDevice, b->stream));
+  B_CUDA(cudaEventRecord(b->amps_copied, b->stream));
+  return ST3D_OK;
+}
+
+int enqueue_persistent(st3d_batch* b, uint32_t steps) {
+  B_CUDA(cudaMemsetAsync(b->d_head, 0, (size_t)steps * sizeof(int), b->stream));
+  for (uint32_t t = 0; t < steps; ++t) {
+    BatchArgs a;
+    a.grids = b->d_grids;
+    a.maps = b->d_maps;
+    a.items = b->d_items;
+    a.total_items = b->total_items;
+    a.n_grids = (int)b->ctx.size();
+    a.head = b->d_head + t;
+    a.amps = b->d_amps;
+    a.step = (int)t;
+    a.timeout_ns = 4000000000ull;
+    a.status = b->d_status;
+    k_batch<<<b->ctas, (kBTJ + 1) * 32, b->smem, b->stream>>>(a);
+    B_CUDA(cudaGetLastError());
+  }
+  return ST3D_OK;
+}
+
+void advance(st3d_batch* b, uint32_t steps) {
+  for (st3d_ctx* c : b->ctx) {
+    c->step += steps;
+    c->launches += steps;
+    if (steps & 1) c->cur ^= 1;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* opts,
+                      st3d_batch** out) {
+  if (!out || !grids || !opts || n == 0) return bfail(ST3D_ERR_INVALID, "null argument or empty batch");
+  *out = nullptr;
+  for (uint32_t gi = 0; gi < n; ++gi) {
+    const st3d_opts& o = opts[gi];
+    if (o.mode != ST3D_MODE_WAVE || o.storage != ST3D_F32 || o.points == 2)
+      return set_error(ST3D_ERR_UNSUPPORTED,
+                       "batch grid %u: the batching form runs the FP32 wave update of 7/13/25 points", gi);
+  }
+  st3d_batch* b = new (std::nothrow) st3d_batch();
+  if (!b) return bfail(ST3D_ERR_NOMEM, "host allocation failed");
+  auto cleanup = [b](int rc) {
+    st3d_batch_destroy(b);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->amps_copied, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(bfail(ST3D_ERR_CUDA, "stream/event creation failed"));
+  }
+  int sm = 0, ccM = 0, ccm = 0;
+  size_t total = 0;
+  int rc = st3d_device_info(&sm, &ccM, &ccm, &total);
+  if (rc != ST3D_OK) return cleanup(rc);
+  b->grids.resize(n);
+  std::vector<CUtensorMap> maps(5 * (size_t)n);
+  for (uint32_t gi = 0; gi < n; ++gi) {
+    st3d_opts o = opts[gi];
+    o.kernel = ST3D_KERNEL_TMA;
+    o.tile_j = kBTJ;
+    o.stages = kBNV;
+    if (o.ichunk <= 0) o.ichunk = 64;  // smaller units balance the shared queue
+    st3d_ctx* c = nullptr;
+    rc = create_context(&grids[gi], &o, b->stream, &c);
+    if (rc != ST3D_OK) return cleanup(rc);
+    b->ctx.push_back(c);
+    BatchGrid& G = b->grids[gi];
+    memset(&G, 0, sizeof G);
+    G.g = c->G;
+    G.cf = c->cf32;
+    G.buf[0] = (float*)c->fld[0];
+    G.buf[1] = (float*)c->fld[1];
+    G.P = o.points;
+    G.R = c->R;
+    G.ntk = c->tma->ntk;
+    G.ntjk = c->tma->ntj * c->tma->ntk;
+    G.ichunk = c->tma->ichunk;
+    G.units = c->tma->units;
+    G.src_i = c->opts.src_i;
+    G.src_j = c->opts.src_j;
+    G.src_k = c->opts.src_k;
+    G.map_base = 5 * (int)gi;
+    maps[5 * gi + 0] = c->tma->umap[0];
+    maps[5 * gi + 1] = c->tma->umap[1];
+    maps[5 * gi + 2] = c->tma->vmap[0];
+    maps[5 * gi + 3] = c->tma->vmap[1];
+    maps[5 * gi + 4] = c->tma->vmap[2];
+    b->points += (uint64_t)grids[gi].xs * grids[gi].ys * grids[gi].zs;
+  }
+  // work items, the most expensive grids first (longest processing time
+  // first keeps the tail short)
+  std::vector<int> order(n);
+  for (uint32_t gi = 0; gi < n; ++gi) order[gi] = (int)gi;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const double wx = (double)b->ctx[x]->grid.xs * b->ctx[x]->grid.ys * b->ctx[x]->grid.zs * (1 + b->grids[x].R);
+    const double wy = (double)b->ctx[y]->grid.xs * b->ctx[y]->grid.ys * b->ctx[y]->grid.zs * (1 + b->grids[y].R);
+    return wx > wy;
+  });
+  std::vector<int2> items;
+  for (int gi : order)
+    for (int u = 0; u < b->grids[gi].units; ++u) items.push_back(make_int2(gi, u));
+  b->total_items = (int)items.size();
+  b->smem = batch_smem_bytes();
+  cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, (kBTJ + 1) * 32, b->smem) !=
+          cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    return cleanup(bfail(ST3D_ERR_UNSUPPORTED, "the batch kernel cannot be resident"));
+  }
+  b->ctas = std::min(sm * per_sm, b->total_items);
+  if (cudaMalloc(&b->d_grids, n * sizeof(BatchGrid)) != cudaSuccess ||
+      cudaMalloc(&b->d_maps, maps.size() * sizeof(CUtensorMap)) != cudaSuccess ||
+      cudaMalloc(&b->d_items, items.size() * sizeof(int2)) != cudaSuccess ||
+      cudaMalloc(&b->d_status, sizeof(uint32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(bfail(ST3D_ERR_NOMEM, "cudaMalloc of the batch tables failed"));
+  }
+  cudaMemcpyAsync(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice,
+                  b->stream);
+  cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                  b->stream);
+  cudaMemsetAsync(b->d_status, 0, sizeof(uint32_t), b->stream);
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return cleanup(bfail(ST3D_ERR_CUDA, "batch set-up failed"));
+  *out = b;
+  return ST3D_OK;
+}
+
+int st3d_batch_destroy(st3d_batch* b) {
+  if (!b) return ST3D_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  destroy_graphs(b);
+  for (st3d_ctx* c : b->ctx) st3d_destroy(c);
+  if (b->d_grids) cudaFree(b->d_grids);
+  if (b->d_maps) cudaFree(b->d_maps);
+  if (b->d_items) cudaFree(b->d_items);
+  if (b->d_head) cudaFree(b->d_head);
+  if (b->d_amps) cudaFree(b->d_amps);
+  if (b->h_amps) cudaFreeHost(b->h_amps);
+  if (b->d_status) cudaFree(b->d_status);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->amps_copied) cudaEventDestroy(b->amps_copied);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return ST3D_OK;
+}
+
+int st3d_batch_context(st3d_batch* b, uint32_t idx, st3d_ctx** ctx) {
+  if (!b || !ctx || idx >= b->ctx.size()) return bfail(ST3D_ERR_INVALID, "bad batch index");
+  *ctx = b->ctx[idx];
+  return ST3D_OK;
+}
+
+int st3d_batch_get_info(const st3d_batch* b, st3d_batch_info* info) {
+  if (!b || !info) return bfail(ST3D_ERR_INVALID, "null argument");
+  memset(info, 0, sizeof *info);
+  info->grids = (uint32_t)b->ctx.size();
+  info->interior_points = b->points;
+  info->work_items = (uint32_t)b->total_items;
+  info->ctas = (uint32_t)b->ctas;
+  info->launches = b->launches;
+  info->graphs = (uint32_t)b->graphs.size();
+  return ST3D_OK;
+}
+
+int st3d_batch_iterate(st3d_batch* b, uint32_t steps, int schedule) {
+  if (!b) return bfail(ST3D_ERR_INVALID, "null batch");
+  if (steps == 0) return ST3D_OK;
+  for (st3d_ctx* c : b->ctx)
+    if (!(c->has_u && c->has_v && c->has_s))
+      return bfail(ST3D_ERR_STATE, "upload or fill u, v and s of every grid before iterating");
+  int rc;
+  if (schedule == ST3D_BATCH_SEQUENTIAL) {
+    for (uint32_t t = 0; t < steps; ++t)
+      for (st3d_ctx* c : b->ctx)
+        if ((rc = st3d_iterate(c, 1)) != ST3D_OK) return rc;
+    b->launches += (uint64_t)steps * b->ctx.size();
+    return ST3D_OK;
+  }
+  if (schedule != ST3D_BATCH_PERSISTENT && schedule != ST3D_BATCH_GRAPH)
+    return bfail(ST3D_ERR_INVALID, "unknown batch schedule");
+  if ((rc = ensure_steps(b, steps)) != ST3D_OK) return rc;
+  if ((rc = stage_call(b, steps)) != ST3D_OK) return rc;
+  if (schedule == ST3D_BATCH_PERSISTENT) {
+    if ((rc = enqueue_persistent(b, steps)) != ST3D_OK) return rc;
+  } else {
+    auto it = b->graphs.find(steps);
+    if (it == b->graphs.end()) {
+      cudaGraph_t graph;
+      B_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      rc = enqueue_persistent(b, steps);
+      cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+      if (rc != ST3D_OK) return rc;
+      if (e != cudaSuccess) return set_error(ST3D_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+      cudaGraphExec_t exec;
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return set_error(ST3D_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+      it = b->graphs.emplace(steps, exec).first;
+    }
+    B_CUDA(cudaGraphLaunch(it->second, b->stream));
+  }
+  b->launches += steps;
+  advance(b, steps);
+  return ST3D_OK;
+}
+
+int st3d_batch_synchronize(st3d_batch* b) {
+  if (!b) return bfail(ST3D_ERR_INVALID, "null batch");
+  B_CUDA(cudaStreamSynchronize(b->stream));
+  uint32_t st = 0;
+  B_CUDA(cudaMemcpy(&st, b->d_status, sizeof st, cudaMemcpyDeviceToHost));
+  if (st != kDevOk) {
+    cudaMemset(b->d_status, 0, sizeof(uint32_t));
+    return set_error(ST3D_ERR_TIMEOUT, "a bounded device wait in the batch kernel gave up (status %u)", st);
+  }
+  for (st3d_ctx* c : b->ctx) {
+    int rc = st3d_synchronize(c);
+    if (rc != ST3D_OK) return rc;
+  }
+  return ST3D_OK;
+}
+
+int st3d_batch_timer_start(st3d_batch* b) {
+  if (!b) return bfail(ST3D_ERR_INVALID, "null batch");
+  B_CUDA(cudaEventRecord(b->ev0, b->stream));
+  return ST3D_OK;
+}
+
+int st3d_batch_timer_stop(st3d_batch* b, float* ms) {
+  if (!b || !ms) return bfail(ST3D_ERR_INVALID, "null argument");
+  B_CUDA(cudaEventRecord(b->ev1, b->stream));
+  B_CUDA(cudaEventSynchronize(b->ev1));
+  B_CUDA(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+  return ST3D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// st3d_ctx.h -- the context behind the C ABI's opaque st3d_ctx handle,
+// shared by the single-grid entry points (st3d_api.cu) and the batch
+// (st3d_batch.cu).
+#pragma once
+
+#include "st3d_internal.h"
+#include "st3d_tma.cuh"
+
+struct st3d_ctx {
+  using Layout = st3d::Layout;
+  using Geom = st3d::Geom;
+  using TmaPlan = st3d::TmaPlan;
+  using Tma16Plan = st3d::Tma16Plan;
+  template <typename C>
+  using Coefs = st3d::Coefs<C>;
+
+  st3d_grid_desc grid;
+  st3d_opts opts;
+  int R = 0;
+  int eb = 0;
+  Layout L;
+  Geom G;
+  void* fld[3] = {nullptr, nullptr, nullptr};  // [0],[1]: u/v pair, [2]: s
+  int cur = 0;                                 // mode W: fld[cur] is u
+  double* scratch = nullptr;                   // norms partials + result
+  unsigned long long* counter = nullptr;       // check()
+  uint32_t* dev_status = nullptr;
+  size_t scratch_doubles = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = true;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint64_t step = 0;
+  uint64_t launches = 0;
+  int kernel = ST3D_KERNEL_SIMPLE;
+  int ichunk = 64;
+  bool has_u = false, has_v = false, has_s = false;
+  int device = 0;
+  TmaPlan* tma = nullptr;
+  // 16-bit storage: low bytes of the u/v buffers (compensated form), scale
+  // exponents (time levels mod 3, then s) and plane maxima (time levels mod 4,
+  // then s), the halo check word, the kernel plan
+  bool f16 = false;
+  void* lo[2] = {nullptr, nullptr};
+  int* E = nullptr;
+  uint32_t* M = nullptr;
+  uint32_t* halo_max = nullptr;
+  Tma16Plan* tma16 = nullptr;
+  float k4 = 0.0f;
+  void* stage = nullptr;      // reference-layout staging buffer for host copies
+  size_t stage_bytes = 0;
+  Coefs<float> cf32;
+  Coefs<double> cf64;
+  size_t bytes = 0;
+};

@@ -109,6 +109,10 @@ enum DeviceStatus : uint32_t {
 // Records a formatted message for st3d_last_error() and returns `status`.
 int set_error(int status, const char* fmt, ...);
 
+// st3d_create on the caller's stream (nullptr: a stream of its own).
+int create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cudaStream_t external,
+                   st3d_ctx** out);
+
 // ---- kernel launchers (st3d_kernels_*.cu) --------------------------------
 // All launch on `stream` and return the cudaGetLastError() of the launch.
 cudaError_t launch_simple(int points, int mode, int storage, const Geom& g, const void* coefs,

@@ -263,6 +263,8 @@ cudaError_t launch_mode(const TmaPlan& plan, const Geom& g, const Coefs<float>& 
     return launch_cfg<P, MODE, 8, 4>(plan, g, cf, v, ubuf, vbuf, sbuf, src, dev_status, stream);
   if (plan.tj == 16 && plan.nv == 2)
     return launch_cfg<P, MODE, 16, 2>(plan, g, cf, v, ubuf, vbuf, sbuf, src, dev_status, stream);
+  if (plan.tj == 16 && plan.nv == 4)
+    return launch_cfg<P, MODE, 16, 4>(plan, g, cf, v, ubuf, vbuf, sbuf, src, dev_status, stream);
   return cudaErrorInvalidConfiguration;
 }
 
@@ -282,6 +284,7 @@ int occupancy_mode(int tj, int nv, size_t smem) {
   if (tj == 8 && nv == 3) n = probe(k_tma<P, MODE, 8, 3>, 9 * 32);
   if (tj == 8 && nv == 4) n = probe(k_tma<P, MODE, 8, 4>, 9 * 32);
   if (tj == 16 && nv == 2) n = probe(k_tma<P, MODE, 16, 2>, 17 * 32);
+  if (tj == 16 && nv == 4) n = probe(k_tma<P, MODE, 16, 4>, 17 * 32);
   cudaGetLastError();
   return n;
 }
@@ -299,8 +302,7 @@ int tma_blocks_per_sm(int points, int mode, int tj, int nv, size_t smem) {
 }
 
 bool tma_config_supported(int tj, int nv) {
-  return (tj == 16 && nv == 3) || (tj == 8 && nv == 3) || (tj == 8 && nv == 4) ||
-         (tj == 16 && nv == 2);
+  return (tj == 16 && (nv == 2 || nv == 3 || nv == 4)) || (tj == 8 && (nv == 3 || nv == 4));
 }
 
 cudaError_t launch_tma(const TmaPlan& plan, int points, int mode, const Geom& g,

@@ -456,10 +456,10 @@ size_t tma16_smem_bytes(int tj, int nv, int R, bool hilo) {
 
 namespace {
 
-template <int KIND, bool HILO, int P>
-cudaError_t launch16_p(const Tma16Plan& pl, const Tma16Args& args, const CUtensorMap* maps,
-                       cudaStream_t stream, int* occupancy_out) {
-  auto kern = k_tma16<KIND, HILO, P, 16, 3>;
+template <int KIND, bool HILO, int P, int NV>
+cudaError_t launch16_nv(const Tma16Plan& pl, const Tma16Args& args, const CUtensorMap* maps,
+                        cudaStream_t stream, int* occupancy_out) {
+  auto kern = k_tma16<KIND, HILO, P, 16, NV>;
   const int threads = 17 * 32;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
   if (e != cudaSuccess) return e;
@@ -468,6 +468,20 @@ cudaError_t launch16_p(const Tma16Plan& pl, const Tma16Args& args, const CUtenso
   }
   kern<<<pl.grid, threads, pl.smem, stream>>>(maps[0], maps[1], maps[2], maps[3], maps[4], args);
   return cudaGetLastError();
+}
+
+// Pipeline depth: a 16-bit stage carries half the bytes of an FP32 stage
+// and is consumed in about half the time, so the ring needs about twice the
+// stages to cover the same DRAM latency.
+template <int KIND, bool HILO, int P>
+cudaError_t launch16_p(const Tma16Plan& pl, const Tma16Args& args, const CUtensorMap* maps,
+                       cudaStream_t stream, int* occupancy_out) {
+  switch (pl.nv) {
+    case 4: return launch16_nv<KIND, HILO, P, 4>(pl, args, maps, stream, occupancy_out);
+    case 6: return launch16_nv<KIND, HILO, P, 6>(pl, args, maps, stream, occupancy_out);
+    case 8: return launch16_nv<KIND, HILO, P, 8>(pl, args, maps, stream, occupancy_out);
+    default: return cudaErrorInvalidConfiguration;
+  }
 }
 
 template <int KIND, bool HILO>
