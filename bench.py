@@ -44,7 +44,12 @@ WORKLOADS = {
     "wave25_528": (25, 528, 528, 528, 4, 5e-4, "uniform"),
     "wave13_1040": (13, 1040, 1040, 1040, 2, 5e-4, "blobs"),
     "wave7_256": (7, 256, 256, 256, 1, 1e-3, "uniform"),
+    "wave7_1024": (7, 1024, 1024, 1024, 4, 1e-3, "blobs"),
+    "wave7_512": (7, 512, 512, 512, 4, 1e-3, "blobs"),
+    "wave13_512": (13, 512, 512, 512, 4, 5e-4, "blobs"),
 }
+# fused steps per pass served for each stencil order
+TB_DEPTHS = {7: (1, 2, 4), 13: (1, 2)}
 SEED = 20251203
 
 
@@ -68,6 +73,10 @@ def parse():
                    help="steps of the batching-form run: 64 seeded grids (0 to skip)")
     p.add_argument("--precision-forms", default="f16_hilo,f16,bf16",
                    help="16-bit storage forms timed and judged against FP64 ('' to skip)")
+    p.add_argument("--temporal-workloads", default="wave7_1024,wave13_1040",
+                   help="workloads timed with 1, 2 and 4 fused steps per pass ('' to skip)")
+    p.add_argument("--temporal-steps", type=int, default=40,
+                   help="timed steps of each temporal-blocking run (a multiple of 4)")
     return p.parse_args()
 
 
@@ -147,11 +156,11 @@ def profile_traffic(kernel_tag, workload):
 
 
 # --------------------------------------------------------------------------
-def make_stencil(S, wl, storage="f32", kernel="auto"):
+def make_stencil(S, wl, storage="f32", kernel="auto", temporal_block=1):
     points, xs, ys, zs, halo, dt, init = WORKLOADS[wl]
     g = S.Grid(xs, ys, zs, halo, halo, halo)
     st = S.Stencil(g, points, "wave", storage, kernel=kernel, dt=dt,
-                   src=(xs // 2, ys // 2, zs // 2))
+                   src=(xs // 2, ys // 2, zs // 2), temporal_block=temporal_block)
     init_fields(S, st, init)
     return g, st
 
@@ -253,6 +262,50 @@ def time_storage(S, wl, storage, steps, warmup, kernel="auto"):
     st.synchronize()
     st.close()
     return g.gvol * steps / (ms * 1e-3) / 1e9, ms / steps, info
+
+
+def temporal_run(S, workloads, steps, warmup, peak):
+    """Throughput of each workload with 1, 2 and 4 leapfrog steps fused per
+    pass over HBM (temporal blocking), and the fused result's agreement with
+    plain steps (bitwise: max |difference| of u after the run)."""
+    out = {}
+    steps = max(4, steps - steps % 4)
+    for wl in workloads:
+        points = WORKLOADS[wl][0]
+        res = {"steps": steps}
+        ref = None
+        for T in TB_DEPTHS.get(points, (1,)):
+            g, st = make_stencil(S, wl, "f32", "tma", temporal_block=T)
+            info = st.info()
+            st.iterate(4 * warmup)  # the same start time for every depth
+            st.synchronize()
+            l0 = st.info().launches
+            st.timer_start()
+            st.iterate(steps)
+            ms = st.timer_stop()
+            st.synchronize()
+            launches = st.info().launches - l0
+            pts = g.gvol
+            ach = info.bytes_per_point * pts * steps / (ms * 1e-3) / 1e9
+            entry = {"value": pts * steps / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+                     "ms_per_step": ms / steps, "launches": int(launches),
+                     "bytes_per_point_step": info.bytes_per_point,
+                     "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
+                                  "frac": ach / peak}}
+            if ref is None:
+                ref = st
+            else:
+                d2, b2, dm, bm = st.norms(S.FIELD_U, ref, S.FIELD_U)
+                entry["max_abs_diff_vs_T1"] = dm
+                st.close()
+            res["T%d" % T] = entry
+        ref.close()
+        base = res["T1"]["value"]
+        for k, e in res.items():
+            if isinstance(e, dict):
+                e["speedup_vs_T1"] = e["value"] / base
+        out[wl] = res
+    return out
 
 
 def e2e_run(S, st, g, calls, iters):
@@ -407,6 +460,10 @@ def run_gb300(args, dist):
 
     if dist.rank == 0 and args.batch_steps > 0:
         result["batch"] = batch_run(S, args.batch_steps, args.warmup)
+
+    tws = [w for w in args.temporal_workloads.split(",") if w]
+    if dist.rank == 0 and tws:
+        result["temporal_blocking"] = temporal_run(S, tws, args.temporal_steps, args.warmup, peak)
 
     host = None
     if args.e2e_calls > 0:

@@ -164,9 +164,20 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves FP32 and 16-bit storage");
   if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves the 7/13/25-point stencils");
-  if (o->temporal_block != 0 && o->temporal_block != 1)
-    return fail(ST3D_ERR_UNSUPPORTED, "temporal blocking depth %d is not available in this build",
+  if (o->temporal_block != 0 && o->temporal_block != 1 && o->temporal_block != 2 &&
+      o->temporal_block != 4)
+    return fail(ST3D_ERR_INVALID, "temporal blocking depth must be 1, 2 or 4 (got %d)",
                 o->temporal_block);
+  if (o->temporal_block > 1 &&
+      (o->mode != ST3D_MODE_WAVE || o->storage != ST3D_F32 || (o->points != 7 && o->points != 13)))
+    return fail(ST3D_ERR_UNSUPPORTED,
+                "temporal blocking fuses FP32 wave steps of the 7- and 13-point stencils");
+  // a level tile loses R columns per fused step at either edge; the tile
+  // keeps 4 columns of margin, so (T - 1) * R <= 4
+  if (o->temporal_block > 1 && (o->temporal_block - 1) * radius_of(o->points) > 4)
+    return fail(ST3D_ERR_UNSUPPORTED,
+                "temporal blocking depth %d is too deep for the %d-point stencil (at most %d)",
+                o->temporal_block, o->points, o->points == 7 ? 4 : 2);
   if (o->mode == ST3D_MODE_WAVE && o->src_i >= 0 &&
       ((uint32_t)o->src_i >= g->xs || o->src_j < 0 || (uint32_t)o->src_j >= g->ys ||
        o->src_k < 0 || (uint32_t)o->src_k >= g->zs))
@@ -233,10 +244,10 @@ int encode_map(CUtensorMap* m, void* base, const Layout& L, uint32_t box_k, uint
   return ST3D_OK;
 }
 
-void* u_ptr(st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->fld[c->cur] : c->fld[0]; }
-void* v_ptr(st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->fld[1 - c->cur] : c->fld[1]; }
-int u_index(const st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? c->cur : 0; }
-int v_index(const st3d_ctx* c) { return c->opts.mode == ST3D_MODE_WAVE ? 1 - c->cur : 1; }
+void* u_ptr(st3d_ctx* c) { return c->fld[c->ub]; }
+void* v_ptr(st3d_ctx* c) { return c->fld[c->vb]; }
+int u_index(const st3d_ctx* c) { return c->ub; }
+int v_index(const st3d_ctx* c) { return c->vb; }
 
 RefGeom ref_geom(const st3d_grid_desc& g) {
   RefGeom R;
@@ -309,14 +320,30 @@ int copy_field_strided(st3d_ctx* c, void* dev, void* host, bool to_device, bool 
 
 // Host (reference layout) -> device field: one contiguous copy into the
 // staging buffer, then a scatter kernel into the library layout (interior,
-// min(halo, 4) planes and rows, all k-halo points up to the row pad).
+// min(halo, 4) planes and rows, all k-halo points up to the row pad).  A
+// context that blocks in time needs a zero halo and checks it here.
 int upload_field(st3d_ctx* c, void* dev, const void* host) {
-  if (!staged_ok(c)) return copy_field_strided(c, dev, const_cast<void*>(host), true, true);
+  if (!staged_ok(c)) {
+    if (c->tb) return fail(ST3D_ERR_UNSUPPORTED, "temporal blocking needs the staged host path (zh <= 32)");
+    return copy_field_strided(c, dev, const_cast<void*>(host), true, true);
+  }
   int rc = ensure_stage(c);
   if (rc != ST3D_OK) return rc;
   ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyHostToDevice, c->stream));
   const st3d_grid_desc& g = c->grid;
   const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4;
+  if (c->tb) {
+    ST3D_CUDA(cudaMemsetAsync(c->halo_max, 0, sizeof(uint32_t), c->stream));
+    cudaError_t e = launch_plane_max_ref(ref_geom(g), (const float*)c->stage, c->M, c->halo_max, hx, hy,
+                                         (int)g.zh, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "halo check kernel");
+    uint32_t halo = 0;
+    ST3D_CUDA(cudaMemcpyAsync(&halo, c->halo_max, sizeof halo, cudaMemcpyDeviceToHost, c->stream));
+    ST3D_CUDA(cudaStreamSynchronize(c->stream));
+    if (halo != 0)
+      return fail(ST3D_ERR_UNSUPPORTED,
+                  "temporal blocking needs a zero halo (a zero Dirichlet boundary)");
+  }
   cudaError_t e = launch_ref_to_dev(c->eb, c->L, ref_geom(g), c->stage, dev, hx, hy, (int)g.zh, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "upload scatter kernel");
   return ST3D_OK;
@@ -491,6 +518,49 @@ FieldRef field_ref(st3d_ctx* c, int f) {
   return r;
 }
 
+// Temporally blocked plan: work units of (16 - 2(T-1)R) rows x 120 columns x
+// ichunk planes; the warm-up of a unit is 2*T*R planes.
+int plan_tb(st3d_ctx* c, int sm_count) {
+  TbPlan* p = new (std::nothrow) TbPlan();
+  if (!p) return fail(ST3D_ERR_NOMEM, "host allocation failed");
+  const int T = c->opts.temporal_block, R = c->R;
+  p->T = T;
+  p->radius = R;
+  p->rows_out = 16 - 2 * (T - 1) * R;
+  int max_smem = 0;
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  if ((int)tb_smem_bytes(c->opts.points, T) > max_smem || p->rows_out < 1) {
+    delete p;
+    return fail(ST3D_ERR_UNSUPPORTED, "temporal blocking of depth %d does not fit", T);
+  }
+  const int per_sm = tb_blocks_per_sm(c->opts.points, T);
+  if (per_sm < 1) {
+    delete p;
+    return fail(ST3D_ERR_UNSUPPORTED, "the temporally blocked kernel cannot be resident");
+  }
+  p->ntj = (int)((c->L.ys + p->rows_out - 1) / p->rows_out);
+  p->ntk = (int)((c->L.zs + 119) / 120);
+  const int ctas = sm_count * per_sm;
+  p->ichunk = c->opts.ichunk > 0 ? c->opts.ichunk
+                                 : tma_pick_ichunk((int)c->L.xs, p->ntj * p->ntk, ctas, 2 * T * R);
+  p->nti = (int)((c->L.xs + p->ichunk - 1) / p->ichunk);
+  p->units = p->ntj * p->ntk * p->nti;
+  p->grid = ctas < p->units ? ctas : p->units;
+  int ok = ST3D_OK;
+  for (int f : {0, 1, 3, 4}) {
+    if (ok == ST3D_OK)
+      ok = encode_map(&p->umap[f], c->fld[f], c->L, kTmaUKW, 16 + 2 * R, kTmaKHalo, c->L.pj);
+    if (ok == ST3D_OK) ok = encode_map(&p->vmap[f], c->fld[f], c->L, kTmaTK, 16, 0, 0);
+  }
+  if (ok == ST3D_OK) ok = encode_map(&p->vmap[2], c->fld[2], c->L, kTmaTK, 16, 0, 0);
+  if (ok != ST3D_OK) {
+    delete p;
+    return ok;
+  }
+  c->tb = p;
+  return ST3D_OK;
+}
+
 int check_device_status(st3d_ctx* c) {
   uint32_t st = 0;
   ST3D_CUDA(cudaMemcpyAsync(&st, c->dev_status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
@@ -631,12 +701,15 @@ int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info
   const int eb = elem_bytes(opts->storage);
   const Layout L = make_layout(grid->xs, grid->ys, grid->zs, eb);
   const int R = radius_of(opts->points);
+  const int T = opts->temporal_block > 0 ? opts->temporal_block : 1;
   info->interior_points = (uint64_t)grid->xs * grid->ys * grid->zs;
-  info->device_bytes = 3 * L.elems() * eb;
+  info->device_bytes = (T > 1 ? 5 : 3) * L.elems() * eb;
   info->nk = L.nk; info->nj = L.nj; info->ni = L.ni;
   info->pk = L.pk; info->pj = L.pj; info->pi = L.pi;
   info->radius = R;
-  info->bytes_per_point = f16_bytes(opts->storage, opts->points, eb);
+  // algorithmic bytes per point and step; a fused pass of T steps reads u,
+  // v, s and writes two levels
+  info->bytes_per_point = T > 1 ? 20.0 / T : f16_bytes(opts->storage, opts->points, eb);
   info->flops_per_point = opts->points == 2 ? 2 : opts->points == 7 ? 12 : opts->points == 13 ? 29 : 41;
   const int tj = opts->tile_j > 0 ? opts->tile_j : 16;
   const bool f16 = eb == 2;
@@ -693,7 +766,8 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
     return status;
   };
   const size_t fbytes = c->L.elems() * c->eb;
-  for (int f = 0; f < 3; ++f) {
+  const int nbuf = c->opts.temporal_block > 1 ? 5 : 3;
+  for (int f = 0; f < nbuf; ++f) {
     cudaError_t e = cudaMalloc(&c->fld[f], fbytes);
     if (e != cudaSuccess) {
       c->fld[f] = nullptr;
@@ -720,9 +794,18 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
     cudaGetLastError();
     return cleanup(fail(ST3D_ERR_CUDA, "stream/event creation failed"));
   }
-  for (int f = 0; f < 3; ++f)
+  for (int f = 0; f < nbuf; ++f)
     if (cudaMemsetAsync(c->fld[f], 0, fbytes, c->stream) != cudaSuccess)
       return cleanup(fail(ST3D_ERR_CUDA, "cudaMemsetAsync failed"));
+  if (nbuf == 5) {
+    if (cudaMalloc(&c->M, grid->xs * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&c->halo_max, sizeof(uint32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      return cleanup(fail(ST3D_ERR_NOMEM, "cudaMalloc of the halo check buffers failed"));
+    }
+    rc = plan_tb(c, sm);
+    if (rc != ST3D_OK) return cleanup(rc);
+  }
   cudaMemsetAsync(c->dev_status, 0, sizeof(uint32_t), c->stream);
 
   c->f16 = c->eb == 2;
@@ -765,7 +848,8 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
     TmaPlan* p = new (std::nothrow) TmaPlan();
     if (p && plan_tma(c, sm, max_smem, p)) {
       int ok = ST3D_OK;
-      for (int f = 0; f < 3 && ok == ST3D_OK; ++f) {
+      for (int f = 0; f < 5 && ok == ST3D_OK; ++f) {
+        if (!c->fld[f]) continue;
         ok = encode_map(&p->umap[f], c->fld[f], c->L, kTmaUKW, p->tj + 2 * c->R, kTmaKHalo,
                         c->L.pj);
         if (ok == ST3D_OK) ok = encode_map(&p->vmap[f], c->fld[f], c->L, kTmaTK, p->tj, 0, 0);
@@ -795,8 +879,9 @@ extern "C" {
 int st3d_destroy(st3d_ctx* c) {
   if (!c) return ST3D_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (int f = 0; f < 3; ++f)
+  for (int f = 0; f < 5; ++f)
     if (c->fld[f]) cudaFree(c->fld[f]);
+  delete c->tb;
   if (c->scratch) cudaFree(c->scratch);
   if (c->counter) cudaFree(c->counter);
   if (c->dev_status) cudaFree(c->dev_status);
@@ -826,7 +911,7 @@ int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
   info->pk = c->L.pk; info->pj = c->L.pj; info->pi = c->L.pi;
   info->kernel = c->kernel;
   info->radius = c->R;
-  info->bytes_per_point = f16_bytes(c->opts.storage, c->opts.points, c->eb);
+  info->bytes_per_point = c->tb ? 20.0 / c->tb->T : f16_bytes(c->opts.storage, c->opts.points, c->eb);
   info->flops_per_point = c->opts.points == 2 ? 2 : c->opts.points == 7 ? 12 : c->opts.points == 13 ? 29 : 41;
   info->tile_j = c->tma ? c->tma->tj : c->tma16 ? c->tma16->tj : 0;
   info->tile_k = (c->tma || c->tma16) ? kTmaTK : 0;
@@ -898,6 +983,28 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
   if (!(c->has_u && c->has_v && c->has_s))
     return fail(ST3D_ERR_STATE, "upload or fill u, v and s before iterating");
   const bool wave = c->opts.mode == ST3D_MODE_WAVE;
+  // fused passes of T steps while at least T remain, then single steps
+  while (c->tb && iterations >= (uint32_t)c->tb->T) {
+    const int T = c->tb->T;
+    Source src;
+    src.i = c->opts.src_i; src.j = c->opts.src_j; src.k = c->opts.src_k;
+    src.amp = 0.0f; src.amp_d = 0.0;
+    float amps[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int t = 0; t < T; ++t)
+      if (src.i >= 0)
+        amps[t] = (float)st3d_ricker((double)(c->step + t) * c->opts.dt, c->opts.src_f, c->opts.src_t0);
+    int o1 = -1, o2 = -1;  // the pair not holding the state
+    for (int b : {0, 1, 3, 4})
+      if (b != c->ub && b != c->vb) (o1 < 0 ? o1 : o2) = b;
+    cudaError_t e = launch_tb(c->opts.points, T, *c->tb, c->G, c->cf32, (float*)c->fld[o1],
+                              (float*)c->fld[o2], c->ub, c->vb, src, amps, c->dev_status, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "temporally blocked kernel launch");
+    c->vb = o1;
+    c->ub = o2;
+    c->step += T;
+    ++c->launches;
+    iterations -= T;
+  }
   for (uint32_t n = 0; n < iterations; ++n) {
     Source src;
     src.i = -1; src.j = -1; src.k = -1; src.amp = 0.0f; src.amp_d = 0.0;
@@ -937,7 +1044,11 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
     if (e != cudaSuccess) return cuda_fail(e, "stencil kernel launch");
     ++c->launches;
     ++c->step;
-    if (wave) c->cur ^= 1;
+    if (wave) {
+      const int t = c->ub;
+      c->ub = c->vb;
+      c->vb = t;
+    }
   }
   return ST3D_OK;
 }
@@ -945,7 +1056,7 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
 int st3d_synchronize(st3d_ctx* c) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   ST3D_CUDA(cudaStreamSynchronize(c->stream));
-  if (c->kernel == ST3D_KERNEL_TMA) return check_device_status(c);
+  if (c->kernel == ST3D_KERNEL_TMA || c->tb) return check_device_status(c);
   return ST3D_OK;
 }
 
@@ -1008,8 +1119,9 @@ int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double 
     ST3D_CUDA(cudaMemsetAsync(M_level(c, 1), 0, c->grid.xs * sizeof(uint32_t), c->stream));
     ST3D_CUDA(cudaMemsetAsync(M_level(c, 2), 0, c->grid.xs * sizeof(uint32_t), c->stream));
   } else {
+    // a context that blocks in time keeps a zero halo
     cudaError_t e = launch_fill(c->opts.storage, c->L, dst, kind, seed, (unsigned)field, a, b, bp,
-                                nb, 0, c->stream);
+                                nb, c->tb ? 1 : 0, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "fill kernel launch");
   }
   if (field == ST3D_FIELD_U) c->has_u = true;

@@ -367,7 +367,7 @@ int stage_call(st3d_batch* b, uint32_t steps) {
   B_CUDA(cudaEventSynchronize(b->amps_copied));
   for (size_t gi = 0; gi < n; ++gi) {
     st3d_ctx* c = b->ctx[gi];
-    b->grids[gi].cur0 = c->cur;
+    b->grids[gi].cur0 = c->ub;
     for (uint32_t t = 0; t < steps; ++t) {
       float amp = 0.0f;
       if (c->opts.src_i >= 0)
@@ -407,7 +407,11 @@ void advance(st3d_batch* b, uint32_t steps) {
   for (st3d_ctx* c : b->ctx) {
     c->step += steps;
     c->launches += steps;
-    if (steps & 1) c->cur ^= 1;
+    if (steps & 1) {
+      const int t = c->ub;
+      c->ub = c->vb;
+      c->vb = t;
+    }
   }
 }
 
@@ -448,6 +452,7 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
     o.kernel = ST3D_KERNEL_TMA;
     o.tile_j = kBTJ;
     o.stages = kBNV;
+    o.temporal_block = 1;  // the batch steps one level at a time
     if (o.ichunk <= 0) o.ichunk = 64;  // smaller units balance the shared queue
     st3d_ctx* c = nullptr;
     rc = create_context(&grids[gi], &o, b->stream, &c);

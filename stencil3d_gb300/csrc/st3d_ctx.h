@@ -11,6 +11,7 @@ struct st3d_ctx {
   using Geom = st3d::Geom;
   using TmaPlan = st3d::TmaPlan;
   using Tma16Plan = st3d::Tma16Plan;
+  using TbPlan = st3d::TbPlan;
   template <typename C>
   using Coefs = st3d::Coefs<C>;
 
@@ -20,8 +21,11 @@ struct st3d_ctx {
   int eb = 0;
   Layout L;
   Geom G;
-  void* fld[3] = {nullptr, nullptr, nullptr};  // [0],[1]: u/v pair, [2]: s
-  int cur = 0;                                 // mode W: fld[cur] is u
+  // [0],[1]: the u/v pair, [2]: s, [3],[4]: the second pair of a context
+  // that blocks in time (a pass writes the other pair)
+  void* fld[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int ub = 0, vb = 1;                          // buffers holding u and v
+  TbPlan* tb = nullptr;
   double* scratch = nullptr;                   // norms partials + result
   unsigned long long* counter = nullptr;       // check()
   uint32_t* dev_status = nullptr;

@@ -167,6 +167,16 @@ cudaError_t launch_dev16_to_ref(int storage, const Layout& L, const RefGeom& R, 
                                 cudaStream_t stream);
 
 // interior_only: points outside the interior are set to 0.
+// Temporal blocking (st3d_kernels_tb.cu): T in {2, 4}, 7 or 13 points.
+struct TbPlan;
+size_t tb_smem_bytes(int points, int T);
+int tb_blocks_per_sm(int points, int T);
+// One pass of T steps: reads the state in buffers ubuf/vbuf, writes U^{n+T-1}
+// to out_prev and U^{n+T} to out_new; amps = the T source amplitudes.
+cudaError_t launch_tb(int points, int T, const TbPlan& pl, const Geom& g, const Coefs<float>& cf,
+                      float* out_prev, float* out_new, int ubuf, int vbuf, const Source& src,
+                      const float* amps, uint32_t* dev_status, cudaStream_t stream);
+
 cudaError_t launch_fill(int storage, const Layout& L, void* dst, int kind, uint64_t seed,
                         unsigned field, double a, double b, const double* blob_params, int nblobs,
                         int interior_only, cudaStream_t stream);

@@ -33,6 +33,8 @@ namespace {
 constexpr int kTK = 128;
 constexpr int kKH16 = 8;               // 16-bit words of k halo either side (16 bytes)
 constexpr int kUKW16 = kTK + 2 * kKH16;  // words per u-tile row
+constexpr int kFRows = 16 + 2 * 4;       // rows of the FP32 centre tile (TJ = 16, R <= 4)
+constexpr int kFTile = kFRows * kUKW16;  // floats per FP32 centre tile
 
 template <int KIND>
 struct Word;
@@ -145,8 +147,10 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
   unsigned char* sr = vr + NV * VSLOT;
   unsigned char* ulr = sr + NV * VSLOT;                 // HILO: centre-plane low bytes of u
   unsigned char* vlr = ulr + (HILO ? NV * LSLOT : 0);   // HILO: low bytes of v
+  // two FP32 copies of the centre u tile, decoded once per step
+  float* ftile = reinterpret_cast<float*>(vlr + (HILO ? NV * LSLOT : 0));
   // the rings end on a 128-byte boundary: barriers, then the stage records
-  uint64_t* full = reinterpret_cast<uint64_t*>(vlr + (HILO ? NV * LSLOT : 0));
+  uint64_t* full = reinterpret_cast<uint64_t*>(ftile + 2 * kFTile);
   uint64_t* empty = full + NV;
   StageInfo* info = reinterpret_cast<StageInfo*>(empty + NV);
   uint32_t* smax = reinterpret_cast<uint32_t*>(info + NV);
@@ -254,11 +258,13 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
         }
       }
     }
-    // Drain: every stage consumed (no copy in flight), maxima flushed.
+    // Drain: no copy in flight (full phases complete), every stage consumed,
+    // maxima flushed.
     if (lane == 0) {
       for (uint32_t m = (h > (uint32_t)NV ? h - NV : 0u); m < h; ++m) {
         const int stage = (int)(m % NV);
-        if (!mbar_wait_bounded(&empty[stage], (m / NV) & 1u, a.timeout_ns)) {
+        const bool landed = mbar_wait_bounded(&full[stage], (m / NV) & 1u, a.timeout_ns);
+        if (!landed || !mbar_wait_bounded(&empty[stage], (m / NV) & 1u, a.timeout_ns)) {
           atomicExch(a.status, (uint32_t)kDevTimeoutEmpty);
           continue;
         }
@@ -271,6 +277,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
   // ---------------- consumers ----------------
   const int r = warp;
   uint32_t h = 0;
+  bool failed = false;
   P4 q[QN];
   for (int unit = blockIdx.x; unit < a.units; unit += gridDim.x) {
     const int ic = unit / a.ntjk;
@@ -291,9 +298,12 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
         if (n >= nsteps) break;
         const uint32_t hh = h + (uint32_t)n;
         const int stage = (int)(hh % NV);
-        if (!mbar_wait_bounded(&full[stage], (hh / NV) & 1u, a.timeout_ns)) {
+        // After a timed-out wait the warp stops waiting but keeps stepping, so
+        // that every consumer warp reaches every named barrier below and the
+        // kernel ends (its results are then void; the status word says so).
+        if (!failed && !mbar_wait_bounded(&full[stage], (hh / NV) & 1u, a.timeout_ns)) {
           atomicExch(a.status, (uint32_t)kDevTimeoutFull);
-          return;
+          failed = true;
         }
         const StageInfo si = info[stage];
         {
@@ -309,15 +319,34 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
                                (r + R) * kUKW16;
           const float sc1 = exp2i(si.e_uc);
           const float2 sc = make_float2(sc1, sc1);
-          const uint2 cw = *reinterpret_cast<const uint2*>(uc + kKH16 + 4 * lane);
-          const P4 L4 = decode4<KIND>(*reinterpret_cast<const uint2*>(uc + 4 + 4 * lane), sc);
-          const P4 C4 = decode4<KIND>(cw, sc);
-          const P4 R4 = decode4<KIND>(*reinterpret_cast<const uint2*>(uc + 12 + 4 * lane), sc);
-          const float w[12] = {L4.a.x, L4.a.y, L4.b.x, L4.b.y, C4.a.x, C4.a.y, C4.b.x, C4.b.y,
-                               R4.a.x, R4.a.y, R4.b.x, R4.b.y};
+          // decode the centre tile once into FP32 (16 B of words per thread),
+          // then every neighbour read is a plain 128-bit FP32 load
+          float* ft = ftile + (hh & 1u) * kFTile;
+          {
+            const int t = r * 32 + lane;
+            constexpr int kChunks = kUKW16 / 8;  // 8 words per chunk
+            if (t < (TJ + 2 * R) * kChunks) {
+              const int row = t / kChunks, c8 = (t - row * kChunks) * 8;
+              const uint4 wv = *reinterpret_cast<const uint4*>(
+                  reinterpret_cast<const uint16_t*>(ur + ((hh - R) % NU) * USLOT) + row * kUKW16 + c8);
+              const P4 d0 = decode4<KIND>(make_uint2(wv.x, wv.y), sc);
+              const P4 d1 = decode4<KIND>(make_uint2(wv.z, wv.w), sc);
+              float* dst = ft + row * kUKW16 + c8;
+              *reinterpret_cast<float4*>(dst) = make_float4(d0.a.x, d0.a.y, d0.b.x, d0.b.y);
+              *reinterpret_cast<float4*>(dst + 4) = make_float4(d1.a.x, d1.a.y, d1.b.x, d1.b.y);
+            }
+          }
+          asm volatile("bar.sync 1, %0;" ::"r"(TJ * 32) : "memory");
+          const float* fc = ft + (r + R) * kUKW16;  // this row; column c is k0 - 8 + c
+          const float4 l4 = *reinterpret_cast<const float4*>(fc + 4 + 4 * lane);
+          const float4 c4 = *reinterpret_cast<const float4*>(fc + kKH16 + 4 * lane);
+          const float4 r4 = *reinterpret_cast<const float4*>(fc + 12 + 4 * lane);
+          const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w,
+                               r4.x, r4.y, r4.z, r4.w};
           // centre values: the word, plus the low byte in the compensated form
-          P4 u0 = C4;
+          P4 u0 = {make_float2(c4.x, c4.y), make_float2(c4.z, c4.w)};
           if (HILO) {
+            const uint2 cw = *reinterpret_cast<const uint2*>(uc + kKH16 + 4 * lane);
             const uint32_t lb = *reinterpret_cast<const uint32_t*>(ulr + stage * LSLOT + r * kTK + 4 * lane);
             const uint16_t cb[4] = {(uint16_t)(cw.x & 0xffff), (uint16_t)(cw.x >> 16),
                                     (uint16_t)(cw.y & 0xffff), (uint16_t)(cw.y >> 16)};
@@ -341,8 +370,10 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
               av = {make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])};
               bv = {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])};
             } else if (ax == 1) {
-              av = decode4<KIND>(*reinterpret_cast<const uint2*>(uc - rr * kUKW16 + kKH16 + 4 * lane), sc);
-              bv = decode4<KIND>(*reinterpret_cast<const uint2*>(uc + rr * kUKW16 + kKH16 + 4 * lane), sc);
+              const float4 A = *reinterpret_cast<const float4*>(fc - rr * kUKW16 + kKH16 + 4 * lane);
+              const float4 B = *reinterpret_cast<const float4*>(fc + rr * kUKW16 + kKH16 + 4 * lane);
+              av = {make_float2(A.x, A.y), make_float2(A.z, A.w)};
+              bv = {make_float2(B.x, B.y), make_float2(B.z, B.w)};
             } else {
               av = q[(ph + 2 * QN - R - rr) % QN];
               bv = q[(ph + QN - R + rr) % QN];
@@ -451,7 +482,8 @@ size_t tma16_smem_bytes(int tj, int nv, int R, bool hilo) {
   const size_t vslot = (size_t)kTK * tj * 2;
   const size_t lslot = (size_t)kTK * tj;
   return (size_t)(nv + R) * uslot + 2 * (size_t)nv * vslot + (hilo ? 2 * (size_t)nv * lslot : 0) +
-         2 * (size_t)nv * 8 + (size_t)nv * sizeof(StageInfo) + 2 * (size_t)nv * 4 + 128;
+         2 * (size_t)kFTile * 4 + 2 * (size_t)nv * 8 + (size_t)nv * sizeof(StageInfo) +
+         2 * (size_t)nv * 4 + 128;
 }
 
 namespace {

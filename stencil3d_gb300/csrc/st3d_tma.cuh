@@ -24,8 +24,8 @@ struct TmaPlan {
   int grid = 0, threads = 0;
   size_t smem = 0;
   uint64_t timeout_ns = 4000000000ull;
-  CUtensorMap umap[3];  // halo box (kTmaUKW x (tj+2R) x 1) over each field buffer
-  CUtensorMap vmap[3];  // interior box (kTmaTK x tj x 1) over each field buffer
+  CUtensorMap umap[5];  // halo box (kTmaUKW x (tj+2R) x 1) over each field buffer
+  CUtensorMap vmap[5];  // interior box (kTmaTK x tj x 1) over each field buffer
 };
 
 // Plan of the 16-bit-storage kernel (st3d_kernels_tma16.cu): same work
@@ -41,6 +41,19 @@ struct Tma16Plan {
   CUtensorMap uhi[2];
   CUtensorMap vhi[3];
   CUtensorMap lo[2];
+};
+
+// Plan of the temporally blocked kernel (st3d_kernels_tb.cu): T fused
+// steps, 16-row level-1 tiles writing rows_out = 16 - 2(T-1)R rows and 120
+// columns; tensor maps over the four state buffers (0, 1, 3, 4) and s (2):
+// umap is the plain kernel's halo box, vmap its interior box.
+struct TbPlan {
+  int T = 2, radius = 0, rows_out = 0;
+  int ichunk = 0, ntj = 0, ntk = 0, nti = 0, units = 0;
+  int grid = 0;
+  uint64_t timeout_ns = 4000000000ull;
+  CUtensorMap umap[5];
+  CUtensorMap vmap[5];
 };
 
 // Planes per work unit: the chunk length that minimises the modelled time

@@ -99,6 +99,11 @@ def test_plan_layout():
     assert two.kernel == S.KERNEL_SIMPLE and two.bytes_per_point == 8.0
     odd = S.plan(S.Grid(17, 19, 23, 4, 4, 1), S.default_opts(7))
     assert (odd.nk * 4) % 128 == 0 and odd.nk >= 32 + 23 + 1
+    # a context that blocks in time holds a second u/v pair: five fields, and
+    # one pass of T steps moves 20 bytes per point
+    tb = S.plan(g, S.default_opts(7, "wave", "f32", temporal_block=4))
+    assert tb.temporal_block == 4 and tb.device_bytes == 5 * 1032 * 1032 * 1088 * 4
+    assert tb.bytes_per_point == 5.0
 
 
 @pytest.mark.parametrize("grid,opts,status", [
@@ -111,6 +116,14 @@ def test_plan_layout():
     ((8, 8, 8, 4, 4, 4), dict(points=2, mode="wave"), S.api.ERR_UNSUPPORTED),
     ((8, 8, 8, 4, 4, 4), dict(points=7, storage="f64", kernel="tma"), S.api.ERR_UNSUPPORTED),
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", src=(8, 0, 0)), S.api.ERR_INVALID),
+    ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", temporal_block=4), S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", temporal_block=2), S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", temporal_block=4), S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", temporal_block=2), S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=7, mode="ref", temporal_block=2), S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", temporal_block=3), S.api.ERR_INVALID),
+    ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", storage="f16", temporal_block=2),
+     S.api.ERR_UNSUPPORTED),
 ])
 def test_plan_rejects_bad_requests(grid, opts, status):
     opts = dict(opts)
