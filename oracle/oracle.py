@@ -245,6 +245,10 @@ def _lib16():
             _u16p, _i32p, _f32p, _u32p, C.c_int, _f32p, C.c_float, C.c_float, C.c_float,
             C.c_void_p, C.c_void_p, C.c_uint]
         L.orc16_iterate_wave.restype = C.c_int
+        L.orc16_iterate_delta.argtypes = [
+            C.c_int, _u16p, _i32p, _f32p, _u16p, _i32p, _f32p, _u16p, _i32p, _f32p, _u32p, C.c_int,
+            _f32p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_uint]
+        L.orc16_iterate_delta.restype = C.c_int
         L.orc16_scale_exponent.argtypes = [C.c_float]
         L.orc16_scale_exponent.restype = C.c_int
         L._f16_ready = True
@@ -297,3 +301,33 @@ def iterate_wave16(u, v, s, grid, points, iterations, c1, c2, src=None, amps=Non
         ampv.ctypes.data if ampv is not None else None, iterations)
     assert rc == 0, rc
     return u, v
+
+
+def delta_fields(u, v, grid, kind):
+    """The FP16 / BF16 storage state of (u, v): Field16 of u and of the time
+    difference d = u - v (FP32 subtraction, as the library forms it)."""
+    u = np.ascontiguousarray(u, np.float32)
+    d = u - np.ascontiguousarray(v, np.float32)
+    return Field16(u, grid, kind, False), Field16(d, grid, kind, False)
+
+
+def delta_decode(fu, fd):
+    """(u, v) of a delta-form state: u = dec(U), v = u - dec(D) (FP32)."""
+    u = fu.decode()
+    return u, u - fd.decode()
+
+
+def iterate_delta16(u, d, s, grid, points, iterations, c1, c2, src=None, amps=None, weights=None):
+    """Mode W in the FP16 / BF16 delta form on Field16 states u, d (in place,
+    newest level afterwards) and s."""
+    if weights is None:
+        weights = wave_weights(points)
+    srcv = None if src is None else np.asarray(src, dtype=np.int64)
+    ampv = None if amps is None else np.ascontiguousarray(amps, dtype=np.float32)
+    rc = _lib16().orc16_iterate_delta(
+        u.kind, u.h, u.E, u.M, d.h, d.E, d.M, s.h, s.E, s.M, gvec(grid), points,
+        np.ascontiguousarray(weights, np.float32), c1, c2, k4_of(points, c1),
+        srcv.ctypes.data if srcv is not None else None,
+        ampv.ctypes.data if ampv is not None else None, iterations)
+    assert rc == 0, rc
+    return u, d

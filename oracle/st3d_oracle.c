@@ -701,3 +701,108 @@ int orc16_iterate_wave(int kind, int hilo, uint16_t* uh, int8_t* uq, int* uE, fl
   }
   return 0;
 }
+
+/* The FP16 / BF16 forms hold u and the time difference d = U^n - U^{n-1}
+ * (the library's st3d_kernels_delta16.cu).  One step:
+ *   scales:  Bd = fmaf(k4, max_{|e|<=R} Mu[i+e], Md[i]);
+ *            Bd = fmaf(c2, Ms[i] + |a|[i == src_i], Bd);  Bu = Mu[i] + Bd
+ *   point:   acc = w_0 (a_0 + b_0); acc = fmaf(w_p, a_p + b_p, acc) ...
+ *            lap = fmaf(m2s, u, acc),  m2s = (float)(-2 sum_p (double)w_p)
+ *            d'  = fmaf(c2, s (+a at the source), fmaf(c1, lap, d))
+ *            D'  = enc(d', Ed'),  u' = u + dec(D'),  U' = enc(u', Eu')
+ *   maxima:  of |u'| and |d'| per plane.
+ * u (uh, uE, uM) and d (dh, dE, dM) are updated in place to the newest
+ * level. */
+int orc16_iterate_delta(int kind, uint16_t* uh, int* uE, float* uM, uint16_t* dh, int* dE,
+                        float* dM, const uint16_t* sh, const int* sE, const float* sM,
+                        const unsigned* g, int points, const float* c, float c1, float c2,
+                        float k4, const long long* src, const float* amp, unsigned iterations) {
+  const orc_layout L = mk_layout(g);
+  const int R = radius_of(points);
+  if (R < 0 || points == 2) return 1;
+  int axis[12], rad[12];
+  const int np = pair_order(points, axis, rad);
+  long long off_m[12], off_p[12];
+  float cf[12];
+  double sw = 0.0;
+  for (int p = 0; p < np; p++) {
+    const long long st = axis[p] == 0 ? (long long)L.imult : axis[p] == 1 ? (long long)L.jmult : 1;
+    off_m[p] = -st * rad[p];
+    off_p[p] = st * rad[p];
+    cf[p] = c[2 + 4 * axis[p] + rad[p] - 1];
+    sw += (double)cf[p];
+  }
+  const float m2s = (float)(-2.0 * sw);
+  const int si = (src && src[0] >= 0) ? (int)src[0] : -1;
+  const long long src_x = si >= 0 ? (long long)(L.ijk_ofs + (size_t)src[0] * L.imult +
+                                                (size_t)src[1] * L.jmult + (size_t)src[2])
+                                  : -1;
+  uint16_t* u2 = (uint16_t*)calloc(L.gsize, sizeof(uint16_t));
+  int* Ebuf = (int*)malloc(3 * (size_t)L.xs * sizeof(int));
+  float* Mbuf = (float*)malloc(3 * (size_t)L.xs * sizeof(float));
+  if (!u2 || !Ebuf || !Mbuf) return 2;
+  int *UE = uE, *UE2 = Ebuf, *DEo = Ebuf + L.xs;
+  float *UM = uM, *UM2 = Mbuf, *DMo = Mbuf + L.xs;
+  uint16_t *Uh = uh, *Uh2 = u2;
+  for (unsigned it = 0; it < iterations; it++) {
+    const float a = amp ? amp[it] : 0.0f;
+    for (unsigned i = 0; i < L.xs; i++) {
+      float nb = 0.0f;
+      for (int e = -R; e <= R; e++) {
+        const long long ii = (long long)i + e;
+        if (ii >= 0 && ii < (long long)L.xs) nb = fmaxf(nb, UM[ii]);
+      }
+      float Bd = fmaf(k4, nb, dM[i]);
+      Bd = fmaf(c2, sM[i] + ((int)i == si ? fabsf(a) : 0.0f), Bd);
+      const float Bu = UM[i] + Bd;
+      DEo[i] = orc16_scale_exponent(Bd);
+      UE2[i] = orc16_scale_exponent(Bu);
+    }
+#pragma omp parallel for schedule(static)
+    for (unsigned i = 0; i < L.xs; i++) {
+      float mu = 0.0f, md = 0.0f;
+      for (unsigned j = 0; j < L.ys; j++)
+        for (unsigned k = 0; k < L.zs; k++) {
+          const size_t x = L.ijk_ofs + (size_t)i * L.imult + (size_t)j * L.jmult + k;
+          float acc = 0.0f;
+          for (int p = 0; p < np; p++) {
+            long long im = i, ip = i;
+            if (axis[p] == 0) { im = (long long)i - rad[p]; ip = (long long)i + rad[p]; }
+            const int em = (im >= 0 && im < (long long)L.xs) ? UE[im] : 0;
+            const int ep = (ip >= 0 && ip < (long long)L.xs) ? UE[ip] : 0;
+            const float sum = w2f(kind, Uh[x + off_m[p]]) * exp2i_f(em) +
+                              w2f(kind, Uh[x + off_p[p]]) * exp2i_f(ep);
+            acc = p == 0 ? cf[0] * sum : fmaf(cf[p], sum, acc);
+          }
+          const float u0 = w2f(kind, Uh[x]) * exp2i_f(UE[i]);
+          const float lap = fmaf(m2s, u0, acc);
+          const float d0 = w2f(kind, dh[x]) * exp2i_f(dE[i]);
+          float s0 = w2f(kind, sh[x]) * exp2i_f(sE[i]);
+          if ((long long)x == src_x) s0 = s0 + a;
+          const float dn = fmaf(c2, s0, fmaf(c1, lap, d0));
+          dh[x] = f2w(kind, dn * exp2i_f(-DEo[i]));
+          const float dq = w2f(kind, dh[x]) * exp2i_f(DEo[i]);
+          const float un = u0 + dq;
+          Uh2[x] = f2w(kind, un * exp2i_f(-UE2[i]));
+          if (fabsf(un) > mu) mu = fabsf(un);
+          if (fabsf(dn) > md) md = fabsf(dn);
+        }
+      UM2[i] = mu;
+      DMo[i] = md;
+    }
+    memcpy(dE, DEo, L.xs * sizeof(int));
+    memcpy(dM, DMo, L.xs * sizeof(float));
+    { uint16_t* t = Uh; Uh = Uh2; Uh2 = t; }
+    { int* t = UE; UE = UE2; UE2 = t; }
+    { float* t = UM; UM = UM2; UM2 = t; }
+  }
+  if (Uh != uh) {
+    memcpy(uh, Uh, L.gsize * sizeof(uint16_t));
+    memcpy(uE, UE, L.xs * sizeof(int));
+    memcpy(uM, UM, L.xs * sizeof(float));
+  }
+  free(u2);
+  free(Ebuf);
+  free(Mbuf);
+  return 0;
+}

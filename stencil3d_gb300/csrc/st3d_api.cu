@@ -67,11 +67,12 @@ int host_elem_bytes(int storage) { return storage == ST3D_F64 ? 8 : 4; }
 
 // Algorithmic HBM bytes per point per step: read u, v, s and write v
 // (config.h:76,82,88 count these 4 streams); 2 points read u and write v
-// (config.h:70).  16-bit storage: 2 bytes per stream (8 B); the compensated
-// form adds the low bytes of the centre u, of v and of the written v (11 B).
+// (config.h:70).  FP16 / BF16 delta form: read u, d, s and write u, d at 2
+// bytes each (10 B); the compensated form: 2-byte u, v, s and written v plus
+// the low bytes of the centre u, of v and of the written v (11 B).
 double f16_bytes(int storage, int points, int eb) {
   if (storage == ST3D_F16_HILO) return 11.0;
-  if (storage == ST3D_F16 || storage == ST3D_BF16) return 8.0;
+  if (storage == ST3D_F16 || storage == ST3D_BF16) return 10.0;
   return (points == 2 ? 2.0 : 4.0) * eb;
 }
 
@@ -164,6 +165,10 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves FP32 and 16-bit storage");
   if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves the 7/13/25-point stencils");
+  if (s16 && o->tile_j != 0 && o->tile_j != 16 &&
+      !(o->tile_j == 8 && (o->storage == ST3D_F16 || o->storage == ST3D_BF16)))
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage runs 16-row tiles (8 also for FP16 / BF16), not %d",
+                o->tile_j);
   if (o->temporal_block != 0 && o->temporal_block != 1 && o->temporal_block != 2 &&
       o->temporal_block != 4)
     return fail(ST3D_ERR_INVALID, "temporal blocking depth must be 1, 2 or 4 (got %d)",
@@ -272,8 +277,8 @@ bool staged_ok(const st3d_ctx* c) {
          g.ys + 8 <= 65535 && g.xs + 8 <= 65535;
 }
 
-int ensure_stage(st3d_ctx* c) {
-  const size_t need = host_array_bytes(c);
+int ensure_stage(st3d_ctx* c, int slots = 1) {
+  const size_t need = host_array_bytes(c) * (size_t)slots;
   if (c->stage && c->stage_bytes >= need) return ST3D_OK;
   if (c->stage) {
     cudaFree(c->stage);
@@ -369,10 +374,16 @@ int download_field(st3d_ctx* c, const void* dev, void* host) {
 }
 
 int mod(long long a, int m) { return (int)(((a % m) + m) % m); }
+// compensated form: scales and maxima of time level `level` (relative to lvl)
 int* E_level(st3d_ctx* c, long long level) { return c->E + (size_t)mod(level, 3) * c->grid.xs; }
 uint32_t* M_level(st3d_ctx* c, long long level) { return c->M + (size_t)mod(level, 4) * c->grid.xs; }
-int* E_s(st3d_ctx* c) { return c->E + 3 * (size_t)c->grid.xs; }
+int* E_s(st3d_ctx* c) { return c->E + 4 * (size_t)c->grid.xs; }
 uint32_t* M_s(st3d_ctx* c) { return c->M + 4 * (size_t)c->grid.xs; }
+// delta form: u per buffer, d per level parity
+int* Eu_buf(st3d_ctx* c, int buf) { return c->E + (size_t)buf * c->grid.xs; }
+uint32_t* Mu_buf(st3d_ctx* c, int buf) { return c->M + (size_t)buf * c->grid.xs; }
+int* Ed_lvl(st3d_ctx* c, uint64_t lvl) { return c->E + (size_t)(2 + (lvl & 1)) * c->grid.xs; }
+uint32_t* Md_lvl(st3d_ctx* c, uint64_t lvl) { return c->M + (size_t)(2 + (lvl & 1)) * c->grid.xs; }
 
 int encode_map_t(CUtensorMap* m, CUtensorMapDataType dt, int eb, void* base, const Layout& L,
                  uint32_t box_k, uint32_t box_j, uint32_t kext, uint32_t jext) {
@@ -396,26 +407,39 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
   const int R = c->R;
   const bool hilo = c->opts.storage == ST3D_F16_HILO;
   p->radius = R;
-  p->tj = 16;
-  // the deepest pipeline that fits (opts.stages may ask for 4, 6 or 8)
+  // The delta form also runs 8-row tiles, two CTAs per SM; by default the
+  // 7- and 13-point stencils do (measured faster at 1024^3), the 25-point
+  // one keeps 16 rows.
+  const int tj_want = c->opts.tile_j > 0 ? c->opts.tile_j : (c->delta && c->opts.points != 25 ? 8 : 16);
+  p->tj = (c->delta && tj_want == 8) ? 8 : 16;
+  p->delta = c->delta;
+  auto smem_of = [&](int nv) {
+    return c->delta ? delta16_smem_bytes(p->tj, nv, R) : tma16_smem_bytes(p->tj, nv, R, hilo);
+  };
+  auto per_sm_of = [&](int nv) {
+    p->nv = nv;
+    p->smem = smem_of(nv);
+    if ((int)p->smem > max_smem) return 0;
+    return c->delta ? delta16_blocks_per_sm(c->opts.storage, c->opts.points, *p)
+                    : tma16_blocks_per_sm(c->opts.storage, c->opts.points, *p);
+  };
+  // the deepest pipeline that keeps the tile's CTAs per SM (two for 8 rows,
+  // one for 16); opts.stages may ask for one depth
   const int want = c->opts.stages;
-  p->nv = 0;
-  for (int nv : {8, 6, 4}) {
+  const int need = p->tj == 8 ? 2 : 1;
+  int per_sm = 0;
+  for (int nv : {12, 8, 6, 4}) {
     if (want && nv != want) continue;
-    if ((int)tma16_smem_bytes(p->tj, nv, R, hilo) <= max_smem) {
-      p->nv = nv;
+    if (nv == 12 && !c->delta) continue;
+    const int b = per_sm_of(nv);
+    if (b >= need || (want && b >= 1)) {
+      per_sm = b;
       break;
     }
   }
-  if (p->nv == 0) {
-    delete p;
-    return fail(ST3D_ERR_UNSUPPORTED, "16-bit kernel does not fit in shared memory");
-  }
-  p->smem = tma16_smem_bytes(p->tj, p->nv, R, hilo);
-  const int per_sm = tma16_blocks_per_sm(c->opts.storage, c->opts.points, *p);
   if (per_sm < 1) {
     delete p;
-    return fail(ST3D_ERR_UNSUPPORTED, "16-bit kernel cannot be resident");
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit kernel does not fit in shared memory");
   }
   p->ntj = (int)((c->L.ys + p->tj - 1) / p->tj);
   p->ntk = (int)((c->L.zs + 127) / 128);
@@ -437,6 +461,7 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
       p->lo[f] = p->vhi[f];  // unused by the uncompensated kernels
   }
   if (ok == ST3D_OK) ok = encode_map_t(&p->vhi[2], w16, 2, c->fld[2], c->L, 128, p->tj, 0, 0);
+  if (ok == ST3D_OK && c->delta) ok = encode_map_t(&p->dmap, w16, 2, c->fld[3], c->L, 128, p->tj, 0, 0);
   if (ok != ST3D_OK) {
     delete p;
     return ok;
@@ -457,8 +482,9 @@ int upload_field16(st3d_ctx* c, int which, const void* host) {
   const st3d_grid_desc& g = c->grid;
   const RefGeom R = ref_geom(g);
   const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4, hz = (int)g.zh;
-  uint32_t* M = which == 0 ? M_level(c, 0) : which == 1 ? M_level(c, -1) : M_s(c);
-  int* E = which == 0 ? E_level(c, 0) : which == 1 ? E_level(c, -1) : E_s(c);
+  const long long n = (long long)c->lvl;
+  uint32_t* M = which == 0 ? M_level(c, n) : which == 1 ? M_level(c, n - 1) : M_s(c);
+  int* E = which == 0 ? E_level(c, n) : which == 1 ? E_level(c, n - 1) : E_s(c);
   const int buf = which == 2 ? 2 : (which == 0 ? u_index(c) : v_index(c));
   ST3D_CUDA(cudaMemsetAsync(M, 0, g.xs * sizeof(uint32_t), c->stream));
   ST3D_CUDA(cudaMemsetAsync(c->halo_max, 0, sizeof(uint32_t), c->stream));
@@ -483,7 +509,7 @@ int download_field16(st3d_ctx* c, int which, void* host) {
   if (rc != ST3D_OK) return rc;
   const st3d_grid_desc& g = c->grid;
   const RefGeom R = ref_geom(g);
-  const long long level = which == 0 ? (long long)c->step : (long long)c->step - 1;
+  const long long level = which == 0 ? (long long)c->lvl : (long long)c->lvl - 1;
   const int buf = which == 0 ? u_index(c) : v_index(c);
   cudaError_t e = launch_dev16_to_ref(c->opts.storage, c->L, R, (const uint16_t*)c->fld[buf],
                                       (const int8_t*)c->lo[buf], E_level(c, level), (float*)c->stage,
@@ -509,13 +535,103 @@ FieldRef field_ref(st3d_ctx* c, int f) {
     }
     return r;
   }
+  if (c->delta) {  // u = dec(U), v = dec(U) - dec(D)
+    r.p = c->fld[c->ub];
+    r.E = Eu_buf(c, c->ub);
+    if (f == ST3D_FIELD_V) {
+      r.p2 = c->fld[3];
+      r.E2 = Ed_lvl(c, c->lvl);
+    }
+    return r;
+  }
   const int buf = f == ST3D_FIELD_U ? u_index(c) : v_index(c);
   r.p = c->fld[buf];
   if (c->f16) {
-    r.E = E_level(c, f == ST3D_FIELD_U ? (long long)c->step : (long long)c->step - 1);
+    r.E = E_level(c, f == ST3D_FIELD_U ? (long long)c->lvl : (long long)c->lvl - 1);
     if (r.storage == ST3D_F16_HILO) r.lo = (const int8_t*)c->lo[buf];
   }
   return r;
+}
+
+// ---- delta form host transfers ----------------------------------------------
+// The staging buffer holds two host arrays: slot 0 = u, slot 1 = v (FP32,
+// reference layout, zero halos).  Setting u or v re-encodes U and/or D = u - v
+// from the pair; the pair is rebuilt from the device state (the values a
+// download returns) when a step or another use of the slots made it stale.
+
+float* stage_slot(st3d_ctx* c, int slot) {
+  return reinterpret_cast<float*>(static_cast<char*>(c->stage) + (size_t)slot * host_array_bytes(c));
+}
+
+// Encode a (or a - b) from the staging slots into 16-bit words with per-plane
+// maxima M and scales E; the halo of a (and b) must be zero.
+int encode_staged16(st3d_ctx* c, const float* a, const float* b, void* words, uint32_t* M, int* E,
+                    const char* what) {
+  const st3d_grid_desc& g = c->grid;
+  const RefGeom R = ref_geom(g);
+  const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4, hz = (int)g.zh;
+  ST3D_CUDA(cudaMemsetAsync(M, 0, g.xs * sizeof(uint32_t), c->stream));
+  ST3D_CUDA(cudaMemsetAsync(c->halo_max, 0, sizeof(uint32_t), c->stream));
+  cudaError_t e = launch_plane_max_ref(R, a, M, c->halo_max, hx, hy, hz, c->stream, b);
+  if (e != cudaSuccess) return cuda_fail(e, "plane maximum kernel");
+  e = launch_ref_to_dev16(c->opts.storage, c->L, R, a, (uint16_t*)words, nullptr, M, E, hx, hy, hz,
+                          c->stream, b);
+  if (e != cudaSuccess) return cuda_fail(e, "16-bit encode kernel");
+  uint32_t halo = 0;
+  ST3D_CUDA(cudaMemcpyAsync(&halo, c->halo_max, sizeof halo, cudaMemcpyDeviceToHost, c->stream));
+  ST3D_CUDA(cudaStreamSynchronize(c->stream));
+  if (halo != 0)
+    return fail(ST3D_ERR_UNSUPPORTED,
+                "16-bit storage needs a zero halo (a zero Dirichlet boundary); %s has nonzero halo values",
+                what);
+  return ST3D_OK;
+}
+
+int delta_rebuild_pair(st3d_ctx* c) {
+  const st3d_grid_desc& g = c->grid;
+  const RefGeom R = ref_geom(g);
+  ST3D_CUDA(cudaMemsetAsync(c->stage, 0, 2 * host_array_bytes(c), c->stream));
+  for (int slot = 0; slot < 2; ++slot) {
+    cudaError_t e = launch_delta_to_ref(c->opts.storage, c->L, R, (const uint16_t*)c->fld[c->ub],
+                                        Eu_buf(c, c->ub), (const uint16_t*)c->fld[3],
+                                        Ed_lvl(c, c->lvl), slot == 1, stage_slot(c, slot), (int)g.zh,
+                                        c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "16-bit decode kernel");
+  }
+  c->pair_valid = true;
+  return ST3D_OK;
+}
+
+// U from slot 0 (when u changed) and D from slot 0 - slot 1.
+int delta_encode_pair(st3d_ctx* c, bool u_changed) {
+  int rc;
+  c->pair_valid = false;
+  if (u_changed &&
+      (rc = encode_staged16(c, stage_slot(c, 0), nullptr, c->fld[c->ub], Mu_buf(c, c->ub),
+                            Eu_buf(c, c->ub), "u")) != ST3D_OK)
+    return rc;
+  if ((rc = encode_staged16(c, stage_slot(c, 0), stage_slot(c, 1), c->fld[3], Md_lvl(c, c->lvl),
+                            Ed_lvl(c, c->lvl), "u or v")) != ST3D_OK)
+    return rc;
+  c->pair_valid = true;
+  return ST3D_OK;
+}
+
+int delta_download(st3d_ctx* c, void* host, bool v) {
+  int rc = ensure_stage(c, 2);
+  if (rc != ST3D_OK) return rc;
+  c->pair_valid = false;
+  const st3d_grid_desc& g = c->grid;
+  const RefGeom R = ref_geom(g);
+  cudaError_t e = launch_delta_to_ref(c->opts.storage, c->L, R, (const uint16_t*)c->fld[c->ub],
+                                      Eu_buf(c, c->ub), (const uint16_t*)c->fld[3], Ed_lvl(c, c->lvl),
+                                      v, stage_slot(c, 0), (int)g.zh, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "16-bit decode kernel");
+  const size_t off = ((size_t)g.xh * R.imult + (size_t)g.yh * R.jmult) * 4;
+  ST3D_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + off, R.imult * 4,
+                              reinterpret_cast<const char*>(stage_slot(c, 0)) + off, R.imult * 4,
+                              (size_t)g.ys * R.jmult * 4, g.xs, cudaMemcpyDeviceToHost, c->stream));
+  return ST3D_OK;
 }
 
 // Temporally blocked plan: work units of (16 - 2(T-1)R) rows x 120 columns x
@@ -703,7 +819,8 @@ int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info
   const int R = radius_of(opts->points);
   const int T = opts->temporal_block > 0 ? opts->temporal_block : 1;
   info->interior_points = (uint64_t)grid->xs * grid->ys * grid->zs;
-  info->device_bytes = (T > 1 ? 5 : 3) * L.elems() * eb;
+  const bool delta = opts->storage == ST3D_F16 || opts->storage == ST3D_BF16;
+  info->device_bytes = (T > 1 ? 5 : delta ? 4 : 3) * L.elems() * eb;
   info->nk = L.nk; info->nj = L.nj; info->ni = L.ni;
   info->pk = L.pk; info->pj = L.pj; info->pi = L.pi;
   info->radius = R;
@@ -766,7 +883,10 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
     return status;
   };
   const size_t fbytes = c->L.elems() * c->eb;
-  const int nbuf = c->opts.temporal_block > 1 ? 5 : 3;
+  // buffers: u/v pair and s; the delta form adds d (3), a context that
+  // blocks in time a second u/v pair (3, 4)
+  c->delta = opts->storage == ST3D_F16 || opts->storage == ST3D_BF16;
+  const int nbuf = c->opts.temporal_block > 1 ? 5 : c->delta ? 4 : 3;
   for (int f = 0; f < nbuf; ++f) {
     cudaError_t e = cudaMalloc(&c->fld[f], fbytes);
     if (e != cudaSuccess) {
@@ -820,18 +940,22 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
           cudaMemsetAsync(c->lo[f], 0, c->L.elems(), c->stream);
         }
       }
-    okm = okm && cudaMalloc(&c->E, 4 * xs * sizeof(int)) == cudaSuccess &&
+    okm = okm && cudaMalloc(&c->E, 5 * xs * sizeof(int)) == cudaSuccess &&
           cudaMalloc(&c->M, 5 * xs * sizeof(uint32_t)) == cudaSuccess &&
           cudaMalloc(&c->halo_max, sizeof(uint32_t)) == cudaSuccess;
     if (!okm) {
       cudaGetLastError();
       return cleanup(fail(ST3D_ERR_NOMEM, "cudaMalloc of the 16-bit storage buffers failed"));
     }
-    cudaMemsetAsync(c->E, 0, 4 * xs * sizeof(int), c->stream);
+    cudaMemsetAsync(c->E, 0, 5 * xs * sizeof(int), c->stream);
     cudaMemsetAsync(c->M, 0, 5 * xs * sizeof(uint32_t), c->stream);
     double wsum = 0.0;
     for (int m = 2; m < 14; ++m) wsum += c->opts.coef[m];
     c->k4 = (float)(4.0 * c->opts.c1 * wsum);
+    // delta form: lap = sum_p w_p (a_p + b_p) + m2s * u
+    double sw = 0.0;
+    for (int p = 0; p < npairs_of(c->opts.points); ++p) sw += (double)c->cf32.cf[p];
+    c->m2s = (float)(-2.0 * sw);
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
     rc = plan_tma16(c, sm, max_smem);
@@ -929,6 +1053,33 @@ int st3d_get_stream(const st3d_ctx* c, void** s) {
 int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   int rc;
+  if (c->delta) {
+    c->step = 0;
+    if ((rc = ensure_stage(c, 2)) != ST3D_OK) return rc;
+    if (u || v) {
+      if (!(u && v) && !c->pair_valid && (rc = delta_rebuild_pair(c)) != ST3D_OK) return rc;
+      c->pair_valid = false;
+      if (u)
+        ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 0), u, host_array_bytes(c), cudaMemcpyHostToDevice,
+                                  c->stream));
+      if (v)
+        ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 1), v, host_array_bytes(c), cudaMemcpyHostToDevice,
+                                  c->stream));
+      if ((rc = delta_encode_pair(c, u != nullptr)) != ST3D_OK) return rc;
+      if (u) c->has_u = true;
+      if (v) c->has_v = true;
+    }
+    if (s) {
+      c->pair_valid = false;  // s passes through slot 0
+      ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 0), s, host_array_bytes(c), cudaMemcpyHostToDevice,
+                                c->stream));
+      if ((rc = encode_staged16(c, stage_slot(c, 0), nullptr, c->fld[2], M_s(c), E_s(c), "s")) !=
+          ST3D_OK)
+        return rc;
+      c->has_s = true;
+    }
+    return ST3D_OK;
+  }
   if (c->f16) {
     c->step = 0;
     if (u) {
@@ -943,8 +1094,8 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
       if ((rc = upload_field16(c, 2, s)) != ST3D_OK) return rc;
       c->has_s = true;
     }
-    ST3D_CUDA(cudaMemsetAsync(M_level(c, 1), 0, c->grid.xs * sizeof(uint32_t), c->stream));
-    ST3D_CUDA(cudaMemsetAsync(M_level(c, 2), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, (long long)c->lvl + 1), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, (long long)c->lvl + 2), 0, c->grid.xs * sizeof(uint32_t), c->stream));
     return ST3D_OK;
   }
   if (u) {
@@ -966,6 +1117,12 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
 int st3d_download(st3d_ctx* c, void* v, void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   int rc;
+  if (c->delta) {
+    if (v && (rc = delta_download(c, v, true)) != ST3D_OK) return rc;
+    if (u && (rc = delta_download(c, u, false)) != ST3D_OK) return rc;
+    ST3D_CUDA(cudaStreamSynchronize(c->stream));
+    return ST3D_OK;
+  }
   if (c->f16) {
     if (v && (rc = download_field16(c, 1, v)) != ST3D_OK) return rc;
     if (u && (rc = download_field16(c, 0, u)) != ST3D_OK) return rc;
@@ -1014,8 +1171,29 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
       src.amp = (float)src.amp_d;
     }
     cudaError_t e;
-    if (c->f16) {
-      const long long n = (long long)c->step;
+    if (c->delta) {
+      Delta16Step st;
+      const int ub = c->ub, un = 1 - c->ub;
+      st.uout = (uint16_t*)c->fld[un];
+      st.d = (uint16_t*)c->fld[3];
+      st.Eu = Eu_buf(c, ub);
+      st.Ed = Ed_lvl(c, c->lvl);
+      st.Es = E_s(c);
+      st.Eu_out = Eu_buf(c, un);
+      st.Ed_out = Ed_lvl(c, c->lvl + 1);
+      st.Mu = Mu_buf(c, ub);
+      st.Md = Md_lvl(c, c->lvl);
+      st.Ms = M_s(c);
+      st.Mu_out = Mu_buf(c, un);
+      st.Md_out = Md_lvl(c, c->lvl + 1);
+      st.k4 = c->k4;
+      st.m2s = c->m2s;
+      st.ubuf = ub;
+      e = launch_delta16(c->opts.storage, c->opts.points, *c->tma16, c->G, c->cf32, st, src,
+                         c->dev_status, c->stream);
+      c->pair_valid = false;
+    } else if (c->f16) {
+      const long long n = (long long)c->lvl;
       Tma16Step st;
       st.vout = (uint16_t*)v_ptr(c);
       st.vlo_out = (int8_t*)c->lo[v_index(c)];
@@ -1044,6 +1222,7 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
     if (e != cudaSuccess) return cuda_fail(e, "stencil kernel launch");
     ++c->launches;
     ++c->step;
+    ++c->lvl;
     if (wave) {
       const int t = c->ub;
       c->ub = c->vb;
@@ -1100,7 +1279,29 @@ int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double 
       bp[4 * q + 3] = 2.0 * unit(4 * q + 3) - 1.0;
     }
   }
-  if (c->f16) {
+  if (c->delta) {
+    // fill the field's staging slot (FP32, reference layout, interior only:
+    // the 16-bit forms keep a zero halo), then encode like an upload
+    int rc = ensure_stage(c, 2);
+    if (rc != ST3D_OK) return rc;
+    if (field != ST3D_FIELD_S && !c->pair_valid && (rc = delta_rebuild_pair(c)) != ST3D_OK) return rc;
+    const st3d_grid_desc& g = c->grid;
+    Layout Lr;
+    Lr.xs = g.xs; Lr.ys = g.ys; Lr.zs = g.zs;
+    Lr.pk = g.zh; Lr.pj = g.yh; Lr.pi = g.xh;
+    Lr.nk = g.zs + 2 * g.zh; Lr.nj = g.ys + 2 * g.yh; Lr.ni = g.xs + 2 * g.xh;
+    c->step = 0;
+    const int slot = field == ST3D_FIELD_V ? 1 : 0;
+    if (field == ST3D_FIELD_S) c->pair_valid = false;  // s passes through slot 0
+    cudaError_t e = launch_fill(ST3D_F32, Lr, stage_slot(c, slot), kind, seed, (unsigned)field, a, b,
+                                bp, nb, 1, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "fill kernel launch");
+    if (field == ST3D_FIELD_S)
+      rc = encode_staged16(c, stage_slot(c, 0), nullptr, c->fld[2], M_s(c), E_s(c), "s");
+    else
+      rc = delta_encode_pair(c, field == ST3D_FIELD_U);
+    if (rc != ST3D_OK) return rc;
+  } else if (c->f16) {
     // fill the float staging buffer (reference layout, interior only: the
     // 16-bit forms keep a zero halo), then encode like an upload
     int rc = ensure_stage(c);
@@ -1116,8 +1317,8 @@ int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double 
     const int which = field == ST3D_FIELD_U ? 0 : field == ST3D_FIELD_V ? 1 : 2;
     c->step = 0;
     if ((rc = upload_field16(c, which, nullptr)) != ST3D_OK) return rc;
-    ST3D_CUDA(cudaMemsetAsync(M_level(c, 1), 0, c->grid.xs * sizeof(uint32_t), c->stream));
-    ST3D_CUDA(cudaMemsetAsync(M_level(c, 2), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, (long long)c->lvl + 1), 0, c->grid.xs * sizeof(uint32_t), c->stream));
+    ST3D_CUDA(cudaMemsetAsync(M_level(c, (long long)c->lvl + 2), 0, c->grid.xs * sizeof(uint32_t), c->stream));
   } else {
     // a context that blocks in time keeps a zero halo
     cudaError_t e = launch_fill(c->opts.storage, c->L, dst, kind, seed, (unsigned)field, a, b, bp,

@@ -40,10 +40,19 @@ struct st3d_ctx {
   bool has_u = false, has_v = false, has_s = false;
   int device = 0;
   TmaPlan* tma = nullptr;
-  // 16-bit storage: low bytes of the u/v buffers (compensated form), scale
-  // exponents (time levels mod 3, then s) and plane maxima (time levels mod 4,
-  // then s), the halo check word, the kernel plan
+  // 16-bit storage.  Compensated form: low bytes of the u/v buffers, scale
+  // exponents E (time levels mod 3; s at 4*xs) and plane maxima M (time
+  // levels mod 4; s at 4*xs).  Delta form (FP16 / BF16): u in buffers 0/1, d
+  // = u^n - u^{n-1} in buffer 3; E and M hold u per buffer (0, 1), d per
+  // level parity (2, 3) and s (4).  `lvl` counts the levels stepped (the
+  // rotation of E and M; `step`, the source time, restarts at each upload);
+  // the staging buffer holds two host arrays for the delta form, whose u/v
+  // pair is valid until a step or another use of the slots.
   bool f16 = false;
+  bool delta = false;
+  bool pair_valid = false;
+  uint64_t lvl = 0;
+  float m2s = 0.0f;
   void* lo[2] = {nullptr, nullptr};
   int* E = nullptr;
   uint32_t* M = nullptr;

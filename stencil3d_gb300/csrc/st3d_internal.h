@@ -149,7 +149,24 @@ struct Tma16Step {
   float k4;
   int ubuf, vbuf;
 };
+// The FP16 / BF16 delta form (st3d_kernels_delta16.cu): u in a pair of
+// buffers, d = u^n - u^{n-1} updated in place.
+struct Delta16Step {
+  uint16_t* uout;                  // buffer receiving u^{n+1}
+  uint16_t* d;                     // d^n in, d^{n+1} out
+  const int *Eu, *Ed, *Es;         // plane scales of u^n, d^n, s
+  int *Eu_out, *Ed_out;            // of u^{n+1}, d^{n+1} (set before the step)
+  const uint32_t *Mu, *Md, *Ms;    // plane maxima of |u^n|, |d^n|, |s|
+  uint32_t *Mu_out, *Md_out;       // maxima of the new levels
+  float k4, m2s;
+  int ubuf;                        // buffer holding u^n
+};
 struct Tma16Plan;
+size_t delta16_smem_bytes(int tj, int nv, int R);
+int delta16_blocks_per_sm(int storage, int points, const Tma16Plan& pl);
+cudaError_t launch_delta16(int storage, int points, const Tma16Plan& pl, const Geom& g,
+                           const Coefs<float>& cf, const Delta16Step& st, const Source& src,
+                           uint32_t* dev_status, cudaStream_t stream);
 size_t tma16_smem_bytes(int tj, int nv, int R, bool hilo);
 int tma16_blocks_per_sm(int storage, int points, const Tma16Plan& pl);
 cudaError_t launch_tma16(int storage, int points, const Tma16Plan& pl, const Geom& g,
@@ -157,11 +174,19 @@ cudaError_t launch_tma16(int storage, int points, const Tma16Plan& pl, const Geo
                          uint32_t* dev_status, cudaStream_t stream);
 
 // 16-bit storage transfers (st3d_kernels_copy.cu).
+// With `stage2`, the field is stage - stage2 (FP32) and the halo check
+// covers both arrays.
 cudaError_t launch_plane_max_ref(const RefGeom& R, const float* stage, uint32_t* M,
-                                 uint32_t* halo_max, int hx, int hy, int hz, cudaStream_t stream);
+                                 uint32_t* halo_max, int hx, int hy, int hz, cudaStream_t stream,
+                                 const float* stage2 = nullptr);
 cudaError_t launch_ref_to_dev16(int storage, const Layout& L, const RefGeom& R, const float* stage,
                                 uint16_t* hi, int8_t* lo, const uint32_t* M, int* E, int hx, int hy,
-                                int hz, cudaStream_t stream);
+                                int hz, cudaStream_t stream, const float* stage2 = nullptr);
+// Delta form -> reference layout: u = dec(U) (minus_d false) or
+// v = dec(U) - dec(D) (minus_d true), interior rows with their k halo.
+cudaError_t launch_delta_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* u,
+                                const int* Eu, const uint16_t* d, const int* Ed, bool minus_d,
+                                float* stage, int hz, cudaStream_t stream);
 cudaError_t launch_dev16_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* hi,
                                 const int8_t* lo, const int* E, float* stage, int hz,
                                 cudaStream_t stream);
@@ -189,6 +214,8 @@ struct FieldRef {
   int storage;
   const int8_t* lo;
   const int* E;
+  const void* p2 = nullptr;  // delta form: the value is dec(p) - dec(p2)
+  const int* E2 = nullptr;
 };
 cudaError_t launch_check(const Geom& g, const FieldRef& v, double expected, double tol,
                          unsigned long long* counter, cudaStream_t stream);

@@ -86,11 +86,16 @@ __device__ __forceinline__ double load_field(const FieldRef& f, long long i, lon
       const uint16_t w = static_cast<const uint16_t*>(f.p)[x];
       float v = __half2float(__ushort_as_half(w));
       if (f.lo) v = __fmaf_rn((float)f.lo[x], ulp256_f16(w), v);
-      return (double)(v * exp2i(f.E[i]));
+      v = v * exp2i(f.E[i]);
+      if (f.p2) v = v - __half2float(__ushort_as_half(static_cast<const uint16_t*>(f.p2)[x])) * exp2i(f.E2[i]);
+      return (double)v;
     }
     case ST3D_BF16: {
       const uint16_t w = static_cast<const uint16_t*>(f.p)[x];
-      return (double)(__uint_as_float((uint32_t)w << 16) * exp2i(f.E[i]));
+      float v = __uint_as_float((uint32_t)w << 16) * exp2i(f.E[i]);
+      if (f.p2)
+        v = v - __uint_as_float((uint32_t)static_cast<const uint16_t*>(f.p2)[x] << 16) * exp2i(f.E2[i]);
+      return (double)v;
     }
     default: return 0.0;
   }

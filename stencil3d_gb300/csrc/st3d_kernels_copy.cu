@@ -103,8 +103,10 @@ __device__ __forceinline__ uint16_t float_to_word(float x) {
 }
 
 // Per-plane maxima of |x| over the interior (float bits, atomicMax) and the
-// maximum over the halo points the stencil reads.
-__global__ void k_plane_max_ref(RefGeom R, const float* __restrict__ stage, uint32_t* __restrict__ M,
+// maximum over the halo points the stencil reads; x = stage - stage2 when
+// stage2 is given (the halo check then covers both arrays).
+__global__ void k_plane_max_ref(RefGeom R, const float* __restrict__ stage,
+                                const float* __restrict__ stage2, uint32_t* __restrict__ M,
                                 uint32_t* __restrict__ halo_max, int hx, int hy, int hz) {
   const int kk = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = (int)blockIdx.y - hy;
@@ -112,9 +114,11 @@ __global__ void k_plane_max_ref(RefGeom R, const float* __restrict__ stage, uint
   const int k = kk - hz;
   float m_in = 0.0f, m_halo = 0.0f;
   if (kk < R.zs + 2 * hz) {
-    const float x = fabsf(stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k]);
+    const long long s = R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k;
+    const float a = stage[s];
+    const float b = stage2 ? stage2[s] : 0.0f;
     const bool inner = i >= 0 && i < R.xs && j >= 0 && j < R.ys && k >= 0 && k < R.zs;
-    if (inner) m_in = x; else m_halo = x;
+    if (inner) m_in = fabsf(a - b); else m_halo = fmaxf(fabsf(a), fabsf(b));
   }
   const uint32_t a = __reduce_max_sync(0xffffffffu, __float_as_uint(m_in));
   const uint32_t b = __reduce_max_sync(0xffffffffu, __float_as_uint(m_halo));
@@ -128,9 +132,9 @@ __global__ void k_plane_max_ref(RefGeom R, const float* __restrict__ stage, uint
 // in the library layout, the plane's scale from its maximum.
 template <int KIND, bool HILO>
 __global__ void k_ref_to_dev16(Layout L, RefGeom R, const float* __restrict__ stage,
-                               uint16_t* __restrict__ hi, int8_t* __restrict__ lo,
-                               const uint32_t* __restrict__ M, int* __restrict__ E, int hx, int hy,
-                               int hz) {
+                               const float* __restrict__ stage2, uint16_t* __restrict__ hi,
+                               int8_t* __restrict__ lo, const uint32_t* __restrict__ M,
+                               int* __restrict__ E, int hx, int hy, int hz) {
   const int kk = blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= R.zs + 2 * hz) return;
   const int j = (int)blockIdx.y - hy;
@@ -139,7 +143,8 @@ __global__ void k_ref_to_dev16(Layout L, RefGeom R, const float* __restrict__ st
   const bool plane_in = i >= 0 && i < R.xs;
   const int e = plane_in ? scale_exponent(__uint_as_float(M[i])) : 0;
   if (plane_in && kk == 0 && blockIdx.y == 0) E[i] = e;
-  const float xs = stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k] * exp2i(-e);
+  const long long s = R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k;
+  const float xs = (stage2 ? stage[s] - stage2[s] : stage[s]) * exp2i(-e);
   const long long d = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
   const uint16_t w = float_to_word<KIND>(xs);
   hi[d] = w;
@@ -171,29 +176,62 @@ __global__ void k_dev16_to_ref(Layout L, RefGeom R, const uint16_t* __restrict__
   stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k] = x * exp2i(E[i]);
 }
 
+// Delta form -> float: u = dec(U), or v = dec(U) - dec(D).
+template <int KIND>
+__global__ void k_delta_to_ref(Layout L, RefGeom R, const uint16_t* __restrict__ u,
+                               const int* __restrict__ Eu, const uint16_t* __restrict__ d,
+                               const int* __restrict__ Ed, bool minus_d, float* __restrict__ stage,
+                               int hz) {
+  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kk >= R.zs + 2 * hz) return;
+  const int j = (int)blockIdx.y;
+  const int i = (int)blockIdx.z;
+  const int k = kk - hz;
+  const long long s = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
+  float x = word_to_float<KIND>(u[s]) * exp2i(Eu[i]);
+  if (minus_d) x = x - word_to_float<KIND>(d[s]) * exp2i(Ed[i]);
+  stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k] = x;
+}
+
 }  // namespace
 
 cudaError_t launch_plane_max_ref(const RefGeom& R, const float* stage, uint32_t* M,
-                                 uint32_t* halo_max, int hx, int hy, int hz, cudaStream_t stream) {
+                                 uint32_t* halo_max, int hx, int hy, int hz, cudaStream_t stream,
+                                 const float* stage2) {
   dim3 block(256);
   dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys + 2 * hy, R.xs + 2 * hx);
   if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
-  k_plane_max_ref<<<grid, block, 0, stream>>>(R, stage, M, halo_max, hx, hy, hz);
+  k_plane_max_ref<<<grid, block, 0, stream>>>(R, stage, stage2, M, halo_max, hx, hy, hz);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ref_to_dev16(int storage, const Layout& L, const RefGeom& R, const float* stage,
                                 uint16_t* hi, int8_t* lo, const uint32_t* M, int* E, int hx, int hy,
-                                int hz, cudaStream_t stream) {
+                                int hz, cudaStream_t stream, const float* stage2) {
   dim3 block(256);
   dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys + 2 * hy, R.xs + 2 * hx);
   if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
   if (storage == ST3D_F16)
-    k_ref_to_dev16<0, false><<<grid, block, 0, stream>>>(L, R, stage, hi, lo, M, E, hx, hy, hz);
+    k_ref_to_dev16<0, false><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz);
   else if (storage == ST3D_BF16)
-    k_ref_to_dev16<1, false><<<grid, block, 0, stream>>>(L, R, stage, hi, lo, M, E, hx, hy, hz);
+    k_ref_to_dev16<1, false><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz);
   else if (storage == ST3D_F16_HILO)
-    k_ref_to_dev16<0, true><<<grid, block, 0, stream>>>(L, R, stage, hi, lo, M, E, hx, hy, hz);
+    k_ref_to_dev16<0, true><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_delta_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* u,
+                                const int* Eu, const uint16_t* d, const int* Ed, bool minus_d,
+                                float* stage, int hz, cudaStream_t stream) {
+  dim3 block(256);
+  dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys, R.xs);
+  if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
+  if (storage == ST3D_F16)
+    k_delta_to_ref<0><<<grid, block, 0, stream>>>(L, R, u, Eu, d, Ed, minus_d, stage, hz);
+  else if (storage == ST3D_BF16)
+    k_delta_to_ref<1><<<grid, block, 0, stream>>>(L, R, u, Eu, d, Ed, minus_d, stage, hz);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

@@ -1,7 +1,10 @@
-// st3d_kernels_tma16.cu -- the precision form: the leapfrog wave step on
-// fields stored in 16 bits with a power-of-two scale per i-plane (FP16 or
-// BF16), optionally with a compensating low byte (FP16 + int8), arithmetic
-// and accumulation in FP32.
+// st3d_kernels_tma16.cu -- the compensated precision form: the leapfrog
+// wave step on u and v stored as FP16 words with a power-of-two scale per
+// i-plane plus a compensating low byte per point (FP16 + int8, ~19
+// significant bits), arithmetic and accumulation in FP32.  (The FP16 / BF16
+// forms without the low byte hold u and the time difference instead of v:
+// st3d_kernels_delta16.cu.)  The kernel keeps the word type as a template
+// parameter; only FP16 words are instantiated.
 //
 // Same structure as the FP32 kernel (st3d_kernels_tma.cu): persistent CTAs
 // over (16-row x 128-point x ichunk-plane) work units, a producer warp
@@ -47,16 +50,6 @@ struct Word<0> {  // FP16
     return __half_as_ushort(__float2half_rn(x));
   }
 };
-template <>
-struct Word<1> {  // BF16
-  static __device__ __forceinline__ float to_float(uint16_t b) {
-    return __uint_as_float((uint32_t)b << 16);
-  }
-  static __device__ __forceinline__ uint16_t from_float(float x) {
-    return __bfloat16_as_ushort(__float2bfloat16_rn(x));
-  }
-};
-
 // Producer-published scales of one stage.
 struct StageInfo {
   int e_up;   // plane entering the queue (i + R)
@@ -527,10 +520,10 @@ cudaError_t launch16_k(int points, const Tma16Plan& pl, const Tma16Args& args, c
   }
 }
 
+// FP16 / BF16 without the low byte run in the delta form
+// (st3d_kernels_delta16.cu); this kernel serves the compensated form.
 cudaError_t dispatch16(int storage, int points, const Tma16Plan& pl, const Tma16Args& args,
                        const CUtensorMap* maps, cudaStream_t stream, int* occ) {
-  if (storage == ST3D_F16) return launch16_k<0, false>(points, pl, args, maps, stream, occ);
-  if (storage == ST3D_BF16) return launch16_k<1, false>(points, pl, args, maps, stream, occ);
   if (storage == ST3D_F16_HILO) return launch16_k<0, true>(points, pl, args, maps, stream, occ);
   return cudaErrorInvalidValue;
 }

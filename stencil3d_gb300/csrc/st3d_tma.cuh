@@ -28,19 +28,22 @@ struct TmaPlan {
   CUtensorMap vmap[5];  // interior box (kTmaTK x tj x 1) over each field buffer
 };
 
-// Plan of the 16-bit-storage kernel (st3d_kernels_tma16.cu): same work
+// Plan of the 16-bit-storage kernels (st3d_kernels_tma16.cu for the
+// compensated form, st3d_kernels_delta16.cu for the delta form): same work
 // decomposition; tensor maps over the 16-bit words of the u/v buffers (halo
-// box and interior box), of s (interior box, index 2), and over the low
-// bytes of the u/v buffers.
+// box and interior box), of s (interior box, index 2), over the low bytes of
+// the u/v buffers, and over d.
 struct Tma16Plan {
   int tj = 16, nv = 3, ichunk = 128, radius = 0;
   int ntj = 0, ntk = 0, nti = 0, units = 0;
   int grid = 0, threads = 0;
   size_t smem = 0;
   uint64_t timeout_ns = 4000000000ull;
+  bool delta = false;     // FP16 / BF16 delta form (st3d_kernels_delta16.cu)
   CUtensorMap uhi[2];
   CUtensorMap vhi[3];
   CUtensorMap lo[2];
+  CUtensorMap dmap;       // delta form: interior box over d (buffer 3)
 };
 
 // Plan of the temporally blocked kernel (st3d_kernels_tb.cu): T fused

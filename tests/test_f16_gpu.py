@@ -1,5 +1,7 @@
-"""GPU parity of the precision form: FP16 / BF16 words with a power-of-two
-scale per i-plane, and FP16 + a compensating byte, all arithmetic in FP32.
+"""GPU parity of the precision forms, all arithmetic in FP32:
+  - FP16 / BF16: u and the time difference d = u^n - u^{n-1} in 16-bit
+    words with a power-of-two scale per i-plane (the delta form);
+  - FP16 + a compensating byte: u and v in FP16 words plus a low byte.
 
 The library's 16-bit kernels and the oracle's restatement of the same
 encoding, scale rule and update must agree bit for bit (decoded u and v
@@ -42,16 +44,29 @@ def test_f16_forms_match_oracle(storage, points, grid, blobs):
         assert st.info().kernel == S.KERNEL_TMA
         uu, vv = u.copy(), v.copy()
         st.iterate_host(vv, s, uu, steps)
+    ou, ov = _oracle_run(storage, u, v, s, grid, points, steps, dt, src)
+    np.testing.assert_array_equal(O.interior(uu, grid), O.interior(ou, grid))
+    np.testing.assert_array_equal(O.interior(vv, grid), O.interior(ov, grid))
+
+
+def _oracle_run(storage, u, v, s, grid, points, steps, dt, src=None, t0=0):
+    """(u, v) after `steps` steps of the oracle's restatement of the form."""
     kind, hilo = O.storage_kind(storage)
     c0, c1, c2 = O.wave_constants(points, 1500.0, dt, 10.0)
-    fu, fv, fs = (O.Field16(x, grid, kind, hilo) for x in (u, v, s))
+    amps = O.ricker_amps(t0, steps, dt)
+    fs = O.Field16(s, grid, kind, hilo and False)
+    if not hilo:
+        fu, fd = O.delta_fields(u, v, grid, kind)
+        O.iterate_delta16(fu, fd, fs, grid, points, steps, np.float32(c1), np.float32(c2), src=src,
+                          amps=amps)
+        return O.delta_decode(fu, fd)
+    fu, fv = (O.Field16(x, grid, kind, hilo) for x in (u, v))
     O.iterate_wave16(fu, fv, fs, grid, points, steps, np.float32(c1), np.float32(c2), src=src,
-                     amps=O.ricker_amps(0, steps, dt))
-    np.testing.assert_array_equal(O.interior(uu, grid), O.interior(fu.decode(), grid))
-    np.testing.assert_array_equal(O.interior(vv, grid), O.interior(fv.decode(), grid))
+                     amps=amps)
+    return fu.decode(), fv.decode()
 
 
-@pytest.mark.parametrize("storage,bound", [("f16_hilo", 3e-4), ("f16", 1e-1), ("bf16", 1.0)])
+@pytest.mark.parametrize("storage,bound", [("f16_hilo", 3e-4), ("f16", 3e-3), ("bf16", 2e-2)])
 def test_f16_forms_track_fp64(storage, bound):
     """Accuracy of each form against FP64 after 60 steps of a smooth field."""
     grid = (32, 36, 140, 4, 4, 4)
@@ -92,3 +107,39 @@ def test_f16_norms_and_fill():
         ui = g.interior(u).astype(np.float64)
         assert np.isclose(e2, np.sum(ui ** 2), rtol=1e-12) and em == np.max(np.abs(ui))
         assert np.all(u[halo_mask(grid)] == 0.0)
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_delta_form_partial_uploads_and_fills(storage):
+    """Setting u or v alone rebuilds the pair from the device state first;
+    fills go through the same path; norms of v decode u - d."""
+    grid = (10, 18, 70, 4, 4, 4)
+    dt = 5e-4
+    v, s, u = _inputs(grid, 21, True)
+    g = S.Grid(*grid)
+    with S.Stencil(g, 13, "wave", storage, dt=dt) as st:
+        st.upload(v, s, u)
+        st.iterate(3)
+        # replace v only: u stays the device's u^3
+        u3, v3 = g.empty(), g.empty()
+        st.download(v3, u3)
+        st.upload(v=v)
+        ua, va = g.empty(), g.empty()
+        st.download(va, ua)
+        np.testing.assert_array_equal(g.interior(ua), g.interior(u3))
+        # v comes back as dec(U) - dec(D) with D = enc(u3 - v)
+        kind, _ = O.storage_kind(storage)
+        _, fd = O.delta_fields(u3, v, grid, kind)
+        np.testing.assert_array_equal(g.interior(va), O.interior(u3 - fd.decode(), grid))
+        # device norms of v decode the same values
+        e2, _, em, _ = st.norms(S.FIELD_V)
+        vi = g.interior(va).astype(np.float64)
+        assert np.isclose(e2, np.sum(vi ** 2), rtol=1e-12) and em == np.max(np.abs(vi))
+        # fills: u blobs, v zero -> d = u
+        st.fill(S.FIELD_U, S.FILL_BLOBS, 5, 3, 4.0)
+        st.fill(S.FIELD_V, S.FILL_CONST, 0, 0.0)
+        ub, vb = g.empty(), g.empty()
+        st.download(vb, ub)
+        assert np.all(g.interior(vb) == 0.0) or np.max(np.abs(g.interior(vb))) <= \
+            2.0 ** -8 * np.max(np.abs(g.interior(ub)))
+        assert np.all(ub[halo_mask(grid)] == 0.0)

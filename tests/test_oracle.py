@@ -15,7 +15,7 @@ import pytest
 
 from oracle import build as obuild
 from oracle import oracle as O
-from tests.helpers import golden_cases, mode_r_inputs, np_dtype, wave_inputs, rel_l2
+from tests.helpers import golden_cases, halo_mask, mode_r_inputs, np_dtype, wave_inputs, rel_l2
 
 META, ARRAYS = golden_cases()
 
@@ -183,3 +183,86 @@ def test_wave_weights_follow_readme_for_seven_points():
     c0, c1, c2 = O.wave_constants(7, 1500.0, 1e-3, 10.0)
     assert abs(c1 - 0.0225) < 1e-15 and abs(c2 - 1e-6) < 1e-18
     assert abs(c0 - (2 - 6 * 0.0225)) < 1e-15
+
+
+# ------------------------------------------------------- 16-bit storage ---
+def _blob_state(grid, seed):
+    u = O.fill_blobs(grid, seed, 4, 6.0)
+    v = (u * np.float32(0.999)).astype(np.float32)
+    v[halo_mask(grid)] = 0.0
+    return u, v
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_delta_form_round_trip(kind):
+    """Encoding u and d = u - v and decoding (u, u - d) loses only the 16-bit
+    rounding of each word: FP16 keeps 11 significant bits, BF16 8."""
+    grid = (10, 12, 40, 4, 4, 4)
+    u, v = _blob_state(grid, 2)
+    fu, fd = O.delta_fields(u, v, grid, kind)
+    uu, vv = O.delta_decode(fu, fd)
+    tol = 2.0 ** -11 if kind == 0 else 2.0 ** -8
+    ui = O.interior(u, grid)
+    assert np.max(np.abs(O.interior(uu, grid) - ui)) <= tol * np.max(np.abs(ui))
+    di = ui - O.interior(v, grid)
+    dd = O.interior(uu, grid) - O.interior(vv, grid)
+    # d is stored at its own scale: its error is relative to |d|, not |u|
+    assert np.max(np.abs(dd - di)) <= 2 * tol * np.max(np.abs(di)) + tol * np.max(np.abs(ui)) * 2.0 ** -11
+
+
+@pytest.mark.parametrize("kind,bound", [(0, 3e-3), (1, 2e-2)])
+def test_delta_form_tracks_fp64(kind, bound):
+    """The FP16 / BF16 delta form against the FP64 leapfrog after 60 steps of
+    a smooth field (25 points): the stated error of the precision form."""
+    grid = (32, 36, 140, 4, 4, 4)
+    dt = 5e-4
+    u, v = _blob_state(grid, 11)
+    s = np.zeros_like(u)
+    c0, c1, c2 = O.wave_constants(25, 1500.0, dt, 10.0)
+    u64, v64 = u.astype(np.float64), v.astype(np.float64)
+    O.iterate_wave(u64, v64, s.astype(np.float64), grid, 25, 60, c0, c1, c2, fma=True)
+    fu, fd = O.delta_fields(u, v, grid, kind)
+    fs = O.Field16(s, grid, kind, False)
+    O.iterate_delta16(fu, fd, fs, grid, 25, 60, np.float32(c1), np.float32(c2))
+    uu, _ = O.delta_decode(fu, fd)
+    assert rel_l2(O.interior(uu, grid), O.interior(u64, grid)) < bound
+
+
+def test_delta_form_is_more_accurate_than_storing_both_levels():
+    """Storing U^{n-1} in FP16 loses the time difference (the velocity) that
+    the delta form keeps: after 100 steps the delta form's error is several
+    times smaller."""
+    grid = (24, 24, 60, 4, 4, 4)
+    dt = 5e-4
+    u, v = _blob_state(grid, 5)
+    s = np.zeros_like(u)
+    c0, c1, c2 = O.wave_constants(13, 1500.0, dt, 10.0)
+    u64, v64 = u.astype(np.float64), v.astype(np.float64)
+    O.iterate_wave(u64, v64, s.astype(np.float64), grid, 13, 100, c0, c1, c2, fma=True)
+    fu, fd = O.delta_fields(u, v, grid, 0)
+    fs = O.Field16(s, grid, 0, False)
+    O.iterate_delta16(fu, fd, fs, grid, 13, 100, np.float32(c1), np.float32(c2))
+    e_delta = rel_l2(O.interior(O.delta_decode(fu, fd)[0], grid), O.interior(u64, grid))
+    # two levels in FP16 words with the same per-plane scales, FP32 arithmetic
+    lu, lv = O.Field16(u, grid, 0, False), O.Field16(v, grid, 0, False)
+    O.iterate_wave16(lu, lv, fs, grid, 13, 100, np.float32(c1), np.float32(c2))
+    e_levels = rel_l2(O.interior(lu.decode(), grid), O.interior(u64, grid))
+    assert e_delta * 4 < e_levels, (e_delta, e_levels)
+
+
+def test_delta_form_scales_hold_a_source():
+    """With a Ricker source the lagged plane scales still bound every value:
+    all words finite, the source plane's d scale follows the amplitude."""
+    grid = (12, 14, 30, 4, 4, 4)
+    dt = 1e-3
+    u = np.zeros(O.shape(grid), np.float32)
+    s = np.zeros_like(u)
+    c0, c1, c2 = O.wave_constants(7, 1500.0, dt, 10.0)
+    src = (6, 7, 15)
+    fu, fd = O.delta_fields(u, u, grid, 0)
+    fs = O.Field16(s, grid, 0, False)
+    amps = O.ricker_amps(0, 120, dt) * np.float32(1e4)
+    O.iterate_delta16(fu, fd, fs, grid, 7, 120, np.float32(c1), np.float32(c2), src=src, amps=amps)
+    uu, vv = O.delta_decode(fu, fd)
+    assert np.all(np.isfinite(uu)) and np.all(np.isfinite(vv))
+    assert np.max(np.abs(O.interior(uu, grid))) > 0
