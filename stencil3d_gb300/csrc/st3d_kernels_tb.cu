@@ -167,6 +167,11 @@ __global__ void __launch_bounds__((kRows + 1) * 32, 1)
     const bool row_in = j >= 0 && j < g.ys;
     const bool out_row = r >= (T - 1) * R && r < kRows - (T - 1) * R && row_in;
     const bool out_col = lane >= 1 && lane <= kOutCols / 4 && kc < g.zs;
+    // interior columns of this lane, and the source's column in it (or -1)
+    bool colv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) colv[c] = row_in && kc + c >= 0 && kc + c < g.zs;
+    const int src_c = (j == a.src_j && (unsigned)(a.src_k - kc) < 4u) ? a.src_k - kc : -1;
     for (int n0 = 0; n0 < nsteps; n0 += QN) {
 #pragma unroll
       for (int ph = 0; ph < QN; ++ph) {
@@ -186,7 +191,11 @@ __global__ void __launch_bounds__((kRows + 1) * 32, 1)
         for (int t = 1; t <= T; ++t) {
           const int pt = p - t * R;
           const bool live = pt >= ia - (T - t) * R && pt < ib + (T - t) * R;
-          if (!live) continue;
+          // level t feeds the output only in rows (t-1)R .. kRows-1-(t-1)R;
+          // the warps of the other rows skip it (their ring rows are never
+          // read by a row that is computed)
+          const bool needed = t == 1 || (r >= (t - 1) * R && r < kRows - (t - 1) * R);
+          if (!live || !needed) continue;
           // centre row of level t-1 at plane pt, its j/k neighbours
           const float* base;
           int pitch_rows_off;
@@ -256,14 +265,18 @@ __global__ void __launch_bounds__((kRows + 1) * 32, 1)
           float ss[4] = {s4.x, s4.y, s4.z, s4.w};
           const bool plane_in = pt >= 0 && pt < g.xs;
           float o[4];
+          if (pt == a.src_i && src_c >= 0) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+              if (c == src_c) ss[c] = ss[c] + a.amp[t - 1];
+          }
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
-            if (pt == a.src_i && j == a.src_j && kc + c == a.src_k) ss[c] = ss[c] + a.amp[t - 1];
             float tt = (w[4 + c] + w[4 + c]) - vv[c];
             tt = __fmaf_rn(a.cf.c1, acc[c], tt);
             o[c] = __fmaf_rn(a.cf.c2, ss[c], tt);
             // outside the interior a level is the zero halo
-            if (!(plane_in && row_in && kc + c >= 0 && kc + c < g.zs)) o[c] = 0.0f;
+            if (!(plane_in && colv[c])) o[c] = 0.0f;
           }
           const float4 o4 = make_float4(o[0], o[1], o[2], o[3]);
           if (t < T) {
