@@ -156,11 +156,11 @@ def profile_traffic(kernel_tag, workload):
 
 
 # --------------------------------------------------------------------------
-def make_stencil(S, wl, storage="f32", kernel="auto", temporal_block=1):
+def make_stencil(S, wl, storage="f32", kernel="auto", temporal_block=1, **kw):
     points, xs, ys, zs, halo, dt, init = WORKLOADS[wl]
     g = S.Grid(xs, ys, zs, halo, halo, halo)
     st = S.Stencil(g, points, "wave", storage, kernel=kernel, dt=dt,
-                   src=(xs // 2, ys // 2, zs // 2), temporal_block=temporal_block)
+                   src=(xs // 2, ys // 2, zs // 2), temporal_block=temporal_block, **kw)
     init_fields(S, st, init)
     return g, st
 
@@ -346,6 +346,7 @@ def e2e_run(S, st, g, calls, iters):
     d2h = 2 * xs * ys * (zs + 2 * g.zhalo) * 4
     return {"value": pts * iters / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "host_path": {0: "auto", 1: "staged", 2: "direct", 3: "strided"}[st.info().host_path],
             "step": "one ITERATE-equivalent call (st3d_iterate_host) of %d time steps" % iters,
             "ms_per_call": ms, "phases": phases,
             "h2d_gbs": h2d / (phases["upload_ms"] * 1e-3) / 1e9,
@@ -471,6 +472,13 @@ def run_gb300(args, dist):
         e2e["value"] = dist.world * e2e["value"] if dist.world > 1 else e2e["value"]
         result["e2e"] = e2e
     st.close()
+    if args.e2e_calls > 0 and result["e2e"]["host_path"] == "direct":
+        # the same calls through the staging buffer, for comparison
+        g2, st2 = make_stencil(S, args.workload, "f32", args.kernel, host_path=S.api.HOST_STAGED)
+        e2s, _ = e2e_run(S, st2, g2, args.e2e_calls, args.e2e_iters)
+        st2.close()
+        result["e2e"]["staged"] = {k: e2s[k] for k in ("value", "ms_per_call", "phases", "h2d_gbs",
+                                                      "d2h_gbs", "host_path")}
 
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and host is not None:
         v_host, u_host = host

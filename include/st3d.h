@@ -64,15 +64,23 @@ typedef enum st3d_mode {
 typedef enum st3d_storage {
   ST3D_F32 = 0,      /* float fields, float arithmetic */
   ST3D_F64 = 1,      /* double fields, double arithmetic (config.h:96-97) */
-  ST3D_F16 = 2,      /* u,v,s stored as FP16 with a per-i-plane power-of-two scale, float arithmetic */
-  ST3D_BF16 = 3,     /* as F16 with bfloat16 storage */
-  ST3D_F16_HILO = 4  /* F16 plus a compensating low FP16 word for each field */
+  /* Mode W only, zero halos.  F16 / BF16 hold u and the time difference
+   * d = u^n - u^{n-1} (not u^{n-1}) as 16-bit words with a power-of-two scale
+   * per i-plane, so the leapfrog velocity keeps 11 (8) significant bits;
+   * float arithmetic; 10 bytes per point per step.  Uploads and downloads
+   * still exchange u and v (v = u - d on the way out). */
+  ST3D_F16 = 2,
+  ST3D_BF16 = 3,
+  /* u and v as FP16 words with a per-plane scale plus a signed byte per point
+   * holding the rounding residual (~19 significant bits); 11 bytes per point
+   * per step. */
+  ST3D_F16_HILO = 4
 } st3d_storage;
 
 typedef enum st3d_kernel {
   ST3D_KERNEL_AUTO = 0,   /* the fastest kernel for the request */
   ST3D_KERNEL_SIMPLE = 1, /* direct-load 2.5D streaming kernel (all storages) */
-  ST3D_KERNEL_TMA = 2     /* TMA-staged 2.5D streaming kernel (F32) */
+  ST3D_KERNEL_TMA = 2     /* TMA-staged 2.5D streaming kernel (F32 and the 16-bit storages) */
 } st3d_kernel;
 
 typedef enum st3d_field {
@@ -94,6 +102,21 @@ typedef struct st3d_grid_desc {
   uint32_t xh, yh, zh; /* halo widths of the caller's host arrays; each >= the stencil radius */
 } st3d_grid_desc;
 
+/* How FP32/FP64 host arrays reach the device.  STAGED: one contiguous copy
+ * into a device staging buffer, then a scatter kernel (a download: a gather
+ * kernel, then one 2-D copy).  DIRECT: the scatter/gather kernels read and
+ * write the host array itself over the host link; it applies to pinned host
+ * arrays (cudaMallocHost, cudaHostAlloc, cudaHostRegister, st3d_host_alloc)
+ * that lie inside one allocation.  AUTO takes DIRECT where it applies.
+ * STRIDED: a 3-D strided copy, used when the host k halo exceeds the device
+ * row pad. */
+typedef enum st3d_host_path {
+  ST3D_HOST_AUTO = 0,
+  ST3D_HOST_STAGED = 1,
+  ST3D_HOST_DIRECT = 2,
+  ST3D_HOST_STRIDED = 3
+} st3d_host_path;
+
 typedef struct st3d_opts {
   int32_t points;   /* 2, 7, 13 or 25 (config.h:35-38 STENCIL_SIZE) */
   int32_t mode;     /* st3d_mode */
@@ -111,7 +134,8 @@ typedef struct st3d_opts {
   int32_t tile_j, tile_k;            /* CTA tile; 0 = automatic */
   int32_t ichunk;                    /* planes per work unit along i; 0 = automatic */
   int32_t stages;                    /* pipeline stages of the TMA kernels; 0 = automatic */
-  int32_t reserved[7];
+  int32_t host_path;                 /* st3d_host_path of FP32/FP64 uploads and downloads */
+  int32_t reserved[6];
 } st3d_opts;
 
 typedef struct st3d_info {
@@ -126,7 +150,8 @@ typedef struct st3d_info {
   double bytes_per_point;     /* algorithmic HBM bytes per point per step */
   double flops_per_point;     /* reference FLOPS_PER_STENCIL (config.h:67-91) */
   int32_t tile_j, tile_k, ichunk, temporal_block;
-  int32_t reserved[8];
+  int32_t host_path;          /* st3d_host_path of the last upload or download */
+  int32_t reserved[7];
 } st3d_info;
 
 typedef struct st3d_ctx st3d_ctx;

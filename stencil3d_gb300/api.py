@@ -23,6 +23,7 @@ F32, F64, F16, BF16, F16_HILO = 0, 1, 2, 3, 4
 KERNEL_AUTO, KERNEL_SIMPLE, KERNEL_TMA = 0, 1, 2
 FIELD_U, FIELD_V, FIELD_S = 0, 1, 2
 FILL_CONST, FILL_UNIFORM, FILL_BLOBS = 0, 1, 2
+HOST_AUTO, HOST_STAGED, HOST_DIRECT, HOST_STRIDED = 0, 1, 2, 3
 
 _MODES = {"ref": MODE_REF, "wave": MODE_WAVE}
 _STORAGES = {"f32": F32, "f64": F64, "f16": F16, "bf16": BF16, "f16_hilo": F16_HILO}
@@ -48,7 +49,8 @@ class Opts(C.Structure):
                 ("pad0", C.c_int32),
                 ("src_f", C.c_double), ("src_t0", C.c_double), ("dt", C.c_double),
                 ("temporal_block", C.c_int32), ("tile_j", C.c_int32), ("tile_k", C.c_int32),
-                ("ichunk", C.c_int32), ("stages", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("ichunk", C.c_int32), ("stages", C.c_int32), ("host_path", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class Info(C.Structure):
@@ -59,7 +61,7 @@ class Info(C.Structure):
                 ("kernel", C.c_int32), ("radius", C.c_int32),
                 ("bytes_per_point", C.c_double), ("flops_per_point", C.c_double),
                 ("tile_j", C.c_int32), ("tile_k", C.c_int32), ("ichunk", C.c_int32),
-                ("temporal_block", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("temporal_block", C.c_int32), ("host_path", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class BatchInfo(C.Structure):

@@ -229,6 +229,21 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
+typedef CUresult (*PFN_pointer_attr)(void*, CUpointer_attribute, CUdeviceptr);
+PFN_pointer_attr get_pointer_attr() {
+  static PFN_pointer_attr fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 4000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_pointer_attr>(f);
+  });
+  return fn;
+}
+
 // Tensor map over one field buffer.  The extents stop where the stencil's
 // valid data stops (dim0 = row front pad + zs + `kext` halo points, dim1 =
 // front rows + ys + `jext` halo rows): box parts beyond them are out of bounds,
@@ -323,23 +338,58 @@ int copy_field_strided(st3d_ctx* c, void* dev, void* host, bool to_device, bool 
   return ST3D_OK;
 }
 
-// Host (reference layout) -> device field: one contiguous copy into the
-// staging buffer, then a scatter kernel into the library layout (interior,
-// min(halo, 4) planes and rows, all k-halo points up to the row pad).  A
+// The device address of a host array the kernels may read and write
+// directly: pinned (cudaMallocHost, cudaHostAlloc, cudaHostRegister) and
+// lying inside one allocation; nullptr otherwise (pageable memory, or a range
+// the driver cannot vouch for), and the transfer then goes through staging.
+void* direct_view(const void* host, size_t bytes) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  auto attr = get_pointer_attr();
+  if (!attr) return nullptr;
+  CUdeviceptr start = 0;
+  size_t size = 0;
+  const CUdeviceptr p = (CUdeviceptr)(uintptr_t)host;
+  if (attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, p) != CUDA_SUCCESS ||
+      attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, p) != CUDA_SUCCESS)
+    return nullptr;
+  if (p < start || p + bytes > start + size) return nullptr;
+  return at.devicePointer;
+}
+
+// Host (reference layout) -> device field.  Staged: one contiguous copy into
+// the staging buffer, then a scatter kernel into the library layout
+// (interior, min(halo, 4) planes and rows, all k-halo points up to the row
+// pad).  Direct: the scatter kernel reads the pinned host array itself.  A
 // context that blocks in time needs a zero halo and checks it here.
 int upload_field(st3d_ctx* c, void* dev, const void* host) {
   if (!staged_ok(c)) {
     if (c->tb) return fail(ST3D_ERR_UNSUPPORTED, "temporal blocking needs the staged host path (zh <= 32)");
+    c->host_path = ST3D_HOST_STRIDED;
     return copy_field_strided(c, dev, const_cast<void*>(host), true, true);
   }
-  int rc = ensure_stage(c);
-  if (rc != ST3D_OK) return rc;
-  ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyHostToDevice, c->stream));
+  const void* src = nullptr;
+  if (c->opts.host_path != ST3D_HOST_STAGED) src = direct_view(host, host_array_bytes(c));
+  if (c->opts.host_path == ST3D_HOST_DIRECT && !src)
+    return fail(ST3D_ERR_INVALID, "the direct host path needs a pinned host array");
+  if (!src) {
+    int rc = ensure_stage(c);
+    if (rc != ST3D_OK) return rc;
+    ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    src = c->stage;
+    c->host_path = ST3D_HOST_STAGED;
+  } else {
+    c->host_path = ST3D_HOST_DIRECT;
+  }
   const st3d_grid_desc& g = c->grid;
   const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4;
   if (c->tb) {
     ST3D_CUDA(cudaMemsetAsync(c->halo_max, 0, sizeof(uint32_t), c->stream));
-    cudaError_t e = launch_plane_max_ref(ref_geom(g), (const float*)c->stage, c->M, c->halo_max, hx, hy,
+    cudaError_t e = launch_plane_max_ref(ref_geom(g), (const float*)src, c->M, c->halo_max, hx, hy,
                                          (int)g.zh, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "halo check kernel");
     uint32_t halo = 0;
@@ -349,20 +399,35 @@ int upload_field(st3d_ctx* c, void* dev, const void* host) {
       return fail(ST3D_ERR_UNSUPPORTED,
                   "temporal blocking needs a zero halo (a zero Dirichlet boundary)");
   }
-  cudaError_t e = launch_ref_to_dev(c->eb, c->L, ref_geom(g), c->stage, dev, hx, hy, (int)g.zh, c->stream);
+  cudaError_t e = launch_ref_to_dev(c->eb, c->L, ref_geom(g), src, dev, hx, hy, (int)g.zh, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "upload scatter kernel");
   return ST3D_OK;
 }
 
 // Device field -> host (reference layout), interior points only: a gather
-// kernel writes every interior row with its k halo into the staging buffer,
-// then one 2-D copy moves per i-plane the span of the ys interior rows.
+// kernel writes every interior row with its k halo, into the pinned host
+// array directly or into the staging buffer followed by one 2-D copy of the
+// span of the ys interior rows of each i-plane.
 int download_field(st3d_ctx* c, const void* dev, void* host) {
-  if (!staged_ok(c)) return copy_field_strided(c, const_cast<void*>(dev), host, false, false);
-  int rc = ensure_stage(c);
-  if (rc != ST3D_OK) return rc;
+  if (!staged_ok(c)) {
+    c->host_path = ST3D_HOST_STRIDED;
+    return copy_field_strided(c, const_cast<void*>(dev), host, false, false);
+  }
   const st3d_grid_desc& g = c->grid;
   const RefGeom R = ref_geom(g);
+  void* dst = nullptr;
+  if (c->opts.host_path != ST3D_HOST_STAGED) dst = direct_view(host, host_array_bytes(c));
+  if (c->opts.host_path == ST3D_HOST_DIRECT && !dst)
+    return fail(ST3D_ERR_INVALID, "the direct host path needs a pinned host array");
+  if (dst) {
+    c->host_path = ST3D_HOST_DIRECT;
+    cudaError_t e = launch_dev_to_ref(c->eb, c->L, R, dev, dst, (int)g.zh, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "download gather kernel");
+    return ST3D_OK;
+  }
+  int rc = ensure_stage(c);
+  if (rc != ST3D_OK) return rc;
+  c->host_path = ST3D_HOST_STAGED;
   cudaError_t e = launch_dev_to_ref(c->eb, c->L, R, dev, c->stage, (int)g.zh, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "download gather kernel");
   const size_t hb = host_elem_bytes(c->opts.storage);
@@ -1041,6 +1106,7 @@ int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
   info->tile_k = (c->tma || c->tma16) ? kTmaTK : 0;
   info->ichunk = c->tma ? c->tma->ichunk : c->tma16 ? c->tma16->ichunk : c->ichunk;
   info->temporal_block = c->opts.temporal_block;
+  info->host_path = c->host_path;
   return ST3D_OK;
 }
 

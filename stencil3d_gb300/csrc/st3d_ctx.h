@@ -60,6 +60,7 @@ struct st3d_ctx {
   Tma16Plan* tma16 = nullptr;
   float k4 = 0.0f;
   void* stage = nullptr;      // reference-layout staging buffer for host copies
+  int host_path = 0;          // st3d_host_path of the last FP32/FP64 transfer
   size_t stage_bytes = 0;
   Coefs<float> cf32;
   Coefs<double> cf64;

@@ -21,39 +21,63 @@ namespace st3d {
 
 namespace {
 
+// Each thread moves kRowUnroll points of a row, blockDim apart, loads first:
+// the host-link path (the source or destination a pinned host array) needs
+// several transfers in flight per thread to cover its latency.
+constexpr int kRowUnroll = 4;
+constexpr int kRowBlock = 256;
+
 template <typename T>
 __global__ void k_ref_to_dev(Layout L, RefGeom R, const T* __restrict__ stage, T* __restrict__ dst,
                              int hx, int hy, int hz) {
   const int klen = R.zs + 2 * hz;
-  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (kk >= klen) return;
+  const int k0 = blockIdx.x * (kRowBlock * kRowUnroll) + threadIdx.x;
   const int j = (int)blockIdx.y - hy;
   const int i = (int)blockIdx.z - hx;
-  const int k = kk - hz;
-  const long long s = R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k;
-  const long long d = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
-  dst[d] = stage[s];
+  const long long srow = R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult - hz;
+  const long long drow = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (int)L.pk - hz;
+  T x[kRowUnroll];
+#pragma unroll
+  for (int m = 0; m < kRowUnroll; ++m) {
+    const int kk = k0 + m * kRowBlock;
+    if (kk < klen) x[m] = stage[srow + kk];
+  }
+#pragma unroll
+  for (int m = 0; m < kRowUnroll; ++m) {
+    const int kk = k0 + m * kRowBlock;
+    if (kk < klen) dst[drow + kk] = x[m];
+  }
 }
 
 template <typename T>
 __global__ void k_dev_to_ref(Layout L, RefGeom R, const T* __restrict__ src, T* __restrict__ stage,
                              int hz) {
   const int klen = R.zs + 2 * hz;
-  const int kk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (kk >= klen) return;
+  const int k0 = blockIdx.x * (kRowBlock * kRowUnroll) + threadIdx.x;
   const int j = (int)blockIdx.y;
   const int i = (int)blockIdx.z;
-  const int k = kk - hz;
-  const long long s = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
-  stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k] = src[s];
+  const long long srow = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (int)L.pk - hz;
+  const long long drow = R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult - hz;
+  T x[kRowUnroll];
+#pragma unroll
+  for (int m = 0; m < kRowUnroll; ++m) {
+    const int kk = k0 + m * kRowBlock;
+    if (kk < klen) x[m] = src[srow + kk];
+  }
+#pragma unroll
+  for (int m = 0; m < kRowUnroll; ++m) {
+    const int kk = k0 + m * kRowBlock;
+    if (kk < klen) stage[drow + kk] = x[m];
+  }
 }
 
 }  // namespace
 
 cudaError_t launch_ref_to_dev(int eb, const Layout& L, const RefGeom& R, const void* stage,
                               void* dst, int hx, int hy, int hz, cudaStream_t stream) {
-  dim3 block(256);
-  dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys + 2 * hy, R.xs + 2 * hx);
+  dim3 block(kRowBlock);
+  dim3 grid((R.zs + 2 * hz + kRowBlock * kRowUnroll - 1) / (kRowBlock * kRowUnroll), R.ys + 2 * hy,
+            R.xs + 2 * hx);
   if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
   if (eb == 4)
     k_ref_to_dev<float><<<grid, block, 0, stream>>>(L, R, (const float*)stage, (float*)dst, hx, hy, hz);
@@ -66,8 +90,8 @@ cudaError_t launch_ref_to_dev(int eb, const Layout& L, const RefGeom& R, const v
 
 cudaError_t launch_dev_to_ref(int eb, const Layout& L, const RefGeom& R, const void* src,
                               void* stage, int hz, cudaStream_t stream) {
-  dim3 block(256);
-  dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys, R.xs);
+  dim3 block(kRowBlock);
+  dim3 grid((R.zs + 2 * hz + kRowBlock * kRowUnroll - 1) / (kRowBlock * kRowUnroll), R.ys, R.xs);
   if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
   if (eb == 4)
     k_dev_to_ref<float><<<grid, block, 0, stream>>>(L, R, (const float*)src, (float*)stage, hz);
