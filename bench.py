@@ -73,6 +73,8 @@ def parse():
                    help="steps of the batching-form run: 64 seeded grids (0 to skip)")
     p.add_argument("--precision-forms", default="f16_hilo,f16,bf16",
                    help="16-bit storage forms timed and judged against FP64 ('' to skip)")
+    p.add_argument("--fp64-steps", type=int, default=5,
+                   help="timed steps of the FP64 (USE_DOUBLE) run of the workload (0 to skip)")
     p.add_argument("--temporal-workloads", default="wave7_1024,wave13_1040",
                    help="workloads timed with 1, 2 and 4 fused steps per pass ('' to skip)")
     p.add_argument("--temporal-steps", type=int, default=40,
@@ -451,6 +453,17 @@ def run_gb300(args, dist):
                                     "bytes_per_point": finfo.bytes_per_point,
                                     "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
                                                  "frac": ach / peak}}
+    if args.fp64_steps > 0:
+        # the reference's USE_DOUBLE build (config.h:96-97) on the device:
+        # the plain kernel in FP64, 32 algorithmic bytes per point
+        gp, msd, dinfo = time_storage(S, args.workload, "f64", args.fp64_steps, min(args.warmup, 3))
+        ach = dinfo.bytes_per_point * pts / (msd * 1e-3) / 1e9
+        result["fp64"] = {"value": dist.world * gp * (ms / ms_max), "unit": "Gpts/s",
+                          "ms_per_step": msd, "bytes_per_point": dinfo.bytes_per_point,
+                          "gflops": pts * dinfo.flops_per_point / (msd * 1e-3) / 1e9,
+                          "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
+                                       "frac": ach / peak},
+                          "kernel": "k_simple<double,%d,wave>" % points}
     if dist.rank == 0 and args.accuracy_steps > 0:
         acc = accuracy_run(S, args.workload, args.accuracy_steps, args.kernel, ["f32"] + forms)
         result["accuracy_vs_fp64"] = acc["f32"]
