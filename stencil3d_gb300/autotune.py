@@ -43,7 +43,7 @@ def candidates(points, mode, storage, zero_halo=False):
                 out.append({"kernel": "tma", "tile_j": tj, "stages": nv})
         return out
     if storage == "f16_hilo":
-        return [{"kernel": "tma", "tile_j": 16, "stages": nv} for nv in (4, 6, 8)]
+        return [{"kernel": "tma", "tile_j": 16, "stages": nv} for nv in (4, 6, 8, 12)]
     if storage == "f64" or points == 2:
         return [{"kernel": "simple", "ichunk": ic} for ic in (32, 64, 128)]
     # FP32: the TMA pipeline shapes the kernel serves, a few unit lengths,

@@ -472,10 +472,9 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
   const int R = c->R;
   const bool hilo = c->opts.storage == ST3D_F16_HILO;
   p->radius = R;
-  // The delta form also runs 8-row tiles, two CTAs per SM; by default the
-  // 7- and 13-point stencils do (measured faster at 1024^3), the 25-point
-  // one keeps 16 rows.
-  const int tj_want = c->opts.tile_j > 0 ? c->opts.tile_j : (c->delta && c->opts.points != 25 ? 8 : 16);
+  // The delta form also runs 8-row tiles, two CTAs per SM (on request; 16
+  // rows measured faster at 1024^3 for every order).
+  const int tj_want = c->opts.tile_j > 0 ? c->opts.tile_j : 16;
   p->tj = (c->delta && tj_want == 8) ? 8 : 16;
   p->delta = c->delta;
   auto smem_of = [&](int nv) {
@@ -489,13 +488,15 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
                     : tma16_blocks_per_sm(c->opts.storage, c->opts.points, *p);
   };
   // the deepest pipeline that keeps the tile's CTAs per SM (two for 8 rows,
-  // one for 16); opts.stages may ask for one depth
+  // one for 16); opts.stages may ask for one depth.  The delta form defaults
+  // to 12 stages for 25 points and 8 otherwise (measured at 1024^3: 25 points
+  // 248 -> 292 Gpts/s from 8 to 12 stages, 7 and 13 points flat or slower).
   const int want = c->opts.stages;
+  const int first = want ? want : c->delta ? (c->opts.points == 25 ? 12 : 8) : 12;
   const int need = p->tj == 8 ? 2 : 1;
   int per_sm = 0;
   for (int nv : {12, 8, 6, 4}) {
-    if (want && nv != want) continue;
-    if (nv == 12 && !c->delta) continue;
+    if (want ? nv != want : nv > first) continue;
     const int b = per_sm_of(nv);
     if (b >= need || (want && b >= 1)) {
       per_sm = b;

@@ -43,8 +43,6 @@ namespace {
 constexpr int kTK = 128;
 constexpr int kKH = 8;                  // 16-bit words of k halo either side (16 bytes)
 constexpr int kUKW = kTK + 2 * kKH;     // words per u-tile row
-// floats of one FP32 centre tile: TJ rows plus R halo rows either side
-__host__ __device__ constexpr int ftile_floats(int TJ, int R) { return (TJ + 2 * R) * kUKW; }
 
 template <int P>
 struct RadD {
@@ -60,7 +58,7 @@ struct StageScales {
   float inv_uo; // plane i of u^{n+1}
   float inv_do; // plane i of d^{n+1}
   float dq;     // plane i of d^{n+1} (decoding it back)
-  float pad;
+  float inv_uc; // 1 / uc
 };
 
 struct Delta16Args {
@@ -87,7 +85,6 @@ __device__ __forceinline__ P4 mul4(const P4& x, float2 c) { return {__fmul2_rn(x
 __device__ __forceinline__ P4 fma4(float2 c, const P4& x, const P4& y) {
   return {__ffma2_rn(c, x.a, y.a), __ffma2_rn(c, x.b, y.b)};
 }
-__device__ __forceinline__ P4 p4(float4 v) { return {make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
 __device__ __forceinline__ float2 splat(float x) { return make_float2(x, x); }
 
 template <int KIND>
@@ -134,14 +131,12 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
   constexpr int USLOT = (kUKW * (TJ + 2 * R) * 2 + 127) / 128 * 128;  // bytes
   constexpr int VSLOT = kTK * TJ * 2;                                  // bytes
   constexpr uint32_t UBYTES = kUKW * (TJ + 2 * R) * 2;
-  constexpr int FTILE = ftile_floats(TJ, R);
 
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* ur = smem;
   unsigned char* dr = ur + NU * USLOT;
   unsigned char* sr = dr + NV * VSLOT;
-  float* ftile = reinterpret_cast<float*>(sr + NV * VSLOT);  // two FP32 centre tiles
-  uint64_t* full = reinterpret_cast<uint64_t*>(ftile + 2 * FTILE);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sr + NV * VSLOT);
   uint64_t* empty = full + NV;
   StageScales* info = reinterpret_cast<StageScales*>(empty + NV);
   uint32_t* smax_u = reinterpret_cast<uint32_t*>(info + NV);
@@ -205,14 +200,15 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
         for (int m = 0; m < cnt; ++m, ++h) {
           StageScales si;
           si.up = exp2i(__shfl_sync(0xffffffffu, e_up, m));
-          si.uc = exp2i(__shfl_sync(0xffffffffu, e_uc, m));
+          const int euc = __shfl_sync(0xffffffffu, e_uc, m);
+          si.uc = exp2i(euc);
+          si.inv_uc = exp2i(-euc);
           si.d = exp2i(__shfl_sync(0xffffffffu, e_d, m));
           si.s = exp2i(__shfl_sync(0xffffffffu, e_s, m));
           si.inv_uo = exp2i(-__shfl_sync(0xffffffffu, e_uo, m));
           const int edo = __shfl_sync(0xffffffffu, e_do, m);
           si.inv_do = exp2i(-edo);
           si.dq = exp2i(edo);
-          si.pad = 0.0f;
           const int n = n0 + m;
           const int stage = (int)(h % NV);
           int good = 1;
@@ -273,16 +269,6 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
   uint32_t h = 0;
   bool failed = false;
   const float2 c1 = splat(a.cf.c1), c2 = splat(a.cf.c2), m2s = splat(a.m2s);
-  // this thread's 8 words of the centre tile to decode each step
-  constexpr int kChunks = kUKW / 8;
-  constexpr int kDec = (TJ + 2 * R) * kChunks;  // chunks of 8 words per tile
-  constexpr int kDecPer = (kDec + TJ * 32 - 1) / (TJ * 32);
-  int dec_off[kDecPer];
-#pragma unroll
-  for (int x = 0; x < kDecPer; ++x) {
-    const int t = r * 32 + lane + x * TJ * 32;
-    dec_off[x] = t < kDec ? (t / kChunks) * kUKW + (t % kChunks) * 8 : -1;
-  }
   P4 q[QN];
   for (int unit = blockIdx.x; unit < a.units; unit += gridDim.x) {
     const int ic = unit / a.ntjk;
@@ -322,54 +308,49 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
         float mu = 0.0f, md = 0.0f;
         if (n >= 2 * R) {
           const int i = ia + n - 2 * R;
-          // decode the centre tile once into FP32 (8 words per thread)
-          float* ft = ftile + (hh & 1u) * FTILE;
-#pragma unroll
-          for (int x = 0; x < kDecPer; ++x) {
-            if (dec_off[x] < 0) continue;
-            const uint4 wv = *reinterpret_cast<const uint4*>(
-                reinterpret_cast<const uint16_t*>(ur + ((hh - R) % NU) * USLOT) + dec_off[x]);
-            const P4 d0 = decode4<KIND>(make_uint2(wv.x, wv.y), si.uc);
-            const P4 d1 = decode4<KIND>(make_uint2(wv.z, wv.w), si.uc);
-            float* dst = ft + dec_off[x];
-            *reinterpret_cast<float4*>(dst) = make_float4(d0.a.x, d0.a.y, d0.b.x, d0.b.y);
-            *reinterpret_cast<float4*>(dst + 4) = make_float4(d1.a.x, d1.a.y, d1.b.x, d1.b.y);
-          }
-          asm volatile("bar.sync 1, %0;" ::"r"(TJ * 32) : "memory");
-          const float* fc = ft + (r + R) * kUKW;  // this row; column c is k0 - 8 + c
-          const float4 l4 = *reinterpret_cast<const float4*>(fc + 4 + 4 * lane);
-          const float4 c4 = *reinterpret_cast<const float4*>(fc + kKH + 4 * lane);
-          const float4 r4 = *reinterpret_cast<const float4*>(fc + 12 + 4 * lane);
-          const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w,
-                               r4.x, r4.y, r4.z, r4.w};
-          const P4 u0 = p4(c4);
+          // Neighbours along j and k come straight from the 16-bit centre
+          // tile; the sum runs in units of the centre plane's scale (the
+          // words themselves) and is scaled once at the end, and the i pairs
+          // (decoded with their own planes' scales) enter multiplied by the
+          // inverse scale.  Power-of-two scaling commutes with every rounding,
+          // so this is bit for bit the sum of scaled values.
+          const uint16_t* row = reinterpret_cast<const uint16_t*>(ur + ((hh - R) % NU) * USLOT) +
+                                (r + R) * kUKW + kKH + 4 * lane;
+          const uint2 wl = *reinterpret_cast<const uint2*>(row - 4);
+          const uint2 wc = *reinterpret_cast<const uint2*>(row);
+          const uint2 wr = *reinterpret_cast<const uint2*>(row + 4);
+          const float2 l01 = w2_to_f2<KIND>(wl.x), l23 = w2_to_f2<KIND>(wl.y);
+          const float2 c01 = w2_to_f2<KIND>(wc.x), c23 = w2_to_f2<KIND>(wc.y);
+          const float2 r01 = w2_to_f2<KIND>(wr.x), r23 = w2_to_f2<KIND>(wr.y);
+          const float w[12] = {l01.x, l01.y, l23.x, l23.y, c01.x, c01.y, c23.x, c23.y,
+                               r01.x, r01.y, r23.x, r23.y};
+          const P4 u0 = {__fmul2_rn(c01, splat(si.uc)), __fmul2_rn(c23, splat(si.uc))};
           P4 acc;
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
             const int ax = pair_axis(P, p);
             const int rr = pair_r(P, p);
-            P4 av, bv;
             P4 sum;
             if (ax == 2 && (rr & 1)) {
               // odd offsets: the operands straddle register pairs, so the
               // sums are formed one point at a time (same rounding)
               sum = {make_float2(w[4 - rr] + w[4 + rr], w[5 - rr] + w[5 + rr]),
                      make_float2(w[6 - rr] + w[6 + rr], w[7 - rr] + w[7 + rr])};
+            } else if (ax == 2) {
+              sum = add4({make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])},
+                         {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])});
+            } else if (ax == 1) {
+              const uint2 A = *reinterpret_cast<const uint2*>(row - rr * kUKW);
+              const uint2 B = *reinterpret_cast<const uint2*>(row + rr * kUKW);
+              sum = add4({w2_to_f2<KIND>(A.x), w2_to_f2<KIND>(A.y)},
+                         {w2_to_f2<KIND>(B.x), w2_to_f2<KIND>(B.y)});
             } else {
-              if (ax == 2) {
-                av = {make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])};
-                bv = {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])};
-              } else if (ax == 1) {
-                av = p4(*reinterpret_cast<const float4*>(fc - rr * kUKW + kKH + 4 * lane));
-                bv = p4(*reinterpret_cast<const float4*>(fc + rr * kUKW + kKH + 4 * lane));
-              } else {
-                av = q[(ph + 2 * QN - R - rr) % QN];
-                bv = q[(ph + QN - R + rr) % QN];
-              }
-              sum = add4(av, bv);
+              sum = mul4(add4(q[(ph + 2 * QN - R - rr) % QN], q[(ph + QN - R + rr) % QN]),
+                         splat(si.inv_uc));
             }
             acc = p == 0 ? mul4(sum, splat(a.cf.cf[p])) : fma4(splat(a.cf.cf[p]), sum, acc);
           }
+          acc = mul4(acc, splat(si.uc));
           const P4 lap = fma4(m2s, u0, acc);
           // d and s of plane i
           const uint2 dw = *reinterpret_cast<const uint2*>(dr + stage * VSLOT + (r * kTK + 4 * lane) * 2);
@@ -502,7 +483,7 @@ cudaError_t dispatch(int storage, int points, const Tma16Plan& pl, const Delta16
 size_t delta16_smem_bytes(int tj, int nv, int R) {
   const size_t uslot = ((size_t)kUKW * (tj + 2 * R) * 2 + 127) / 128 * 128;
   const size_t vslot = (size_t)kTK * tj * 2;
-  return (size_t)(nv + R) * uslot + 2 * (size_t)nv * vslot + 2 * (size_t)ftile_floats(tj, R) * 4 +
+  return (size_t)(nv + R) * uslot + 2 * (size_t)nv * vslot +
          2 * (size_t)nv * 8 + (size_t)nv * sizeof(StageScales) + 3 * (size_t)nv * 4 + 128;
 }
 

@@ -36,8 +36,6 @@ namespace {
 constexpr int kTK = 128;
 constexpr int kKH16 = 8;               // 16-bit words of k halo either side (16 bytes)
 constexpr int kUKW16 = kTK + 2 * kKH16;  // words per u-tile row
-constexpr int kFRows = 16 + 2 * 4;       // rows of the FP32 centre tile (TJ = 16, R <= 4)
-constexpr int kFTile = kFRows * kUKW16;  // floats per FP32 centre tile
 
 template <int KIND>
 struct Word;
@@ -101,6 +99,16 @@ __device__ __forceinline__ P4 fma4(float2 c, const P4& x, const P4& y) {
   return {__ffma2_rn(c, x.a, y.a), __ffma2_rn(c, x.b, y.b)};
 }
 
+// 4 words -> 4 floats, unscaled
+template <int KIND>
+__device__ __forceinline__ P4 words4(uint2 w) {
+  if (KIND == 0)
+    return {__half22float2(*reinterpret_cast<const __half2*>(&w.x)),
+            __half22float2(*reinterpret_cast<const __half2*>(&w.y))};
+  return {__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w.x)),
+          __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w.y))};
+}
+
 template <int KIND>
 __device__ __forceinline__ P4 decode4(uint2 w, float2 sc) {
   float2 lo, hi;
@@ -140,10 +148,8 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
   unsigned char* sr = vr + NV * VSLOT;
   unsigned char* ulr = sr + NV * VSLOT;                 // HILO: centre-plane low bytes of u
   unsigned char* vlr = ulr + (HILO ? NV * LSLOT : 0);   // HILO: low bytes of v
-  // two FP32 copies of the centre u tile, decoded once per step
-  float* ftile = reinterpret_cast<float*>(vlr + (HILO ? NV * LSLOT : 0));
   // the rings end on a 128-byte boundary: barriers, then the stage records
-  uint64_t* full = reinterpret_cast<uint64_t*>(ftile + 2 * kFTile);
+  uint64_t* full = reinterpret_cast<uint64_t*>(vlr + (HILO ? NV * LSLOT : 0));
   uint64_t* empty = full + NV;
   StageInfo* info = reinterpret_cast<StageInfo*>(empty + NV);
   uint32_t* smax = reinterpret_cast<uint32_t*>(info + NV);
@@ -312,37 +318,27 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
                                (r + R) * kUKW16;
           const float sc1 = exp2i(si.e_uc);
           const float2 sc = make_float2(sc1, sc1);
-          // decode the centre tile once into FP32 (16 B of words per thread),
-          // then every neighbour read is a plain 128-bit FP32 load
-          float* ft = ftile + (hh & 1u) * kFTile;
-          {
-            const int t = r * 32 + lane;
-            constexpr int kChunks = kUKW16 / 8;  // 8 words per chunk
-            if (t < (TJ + 2 * R) * kChunks) {
-              const int row = t / kChunks, c8 = (t - row * kChunks) * 8;
-              const uint4 wv = *reinterpret_cast<const uint4*>(
-                  reinterpret_cast<const uint16_t*>(ur + ((hh - R) % NU) * USLOT) + row * kUKW16 + c8);
-              const P4 d0 = decode4<KIND>(make_uint2(wv.x, wv.y), sc);
-              const P4 d1 = decode4<KIND>(make_uint2(wv.z, wv.w), sc);
-              float* dst = ft + row * kUKW16 + c8;
-              *reinterpret_cast<float4*>(dst) = make_float4(d0.a.x, d0.a.y, d0.b.x, d0.b.y);
-              *reinterpret_cast<float4*>(dst + 4) = make_float4(d1.a.x, d1.a.y, d1.b.x, d1.b.y);
-            }
-          }
-          asm volatile("bar.sync 1, %0;" ::"r"(TJ * 32) : "memory");
-          const float* fc = ft + (r + R) * kUKW16;  // this row; column c is k0 - 8 + c
-          const float4 l4 = *reinterpret_cast<const float4*>(fc + 4 + 4 * lane);
-          const float4 c4 = *reinterpret_cast<const float4*>(fc + kKH16 + 4 * lane);
-          const float4 r4 = *reinterpret_cast<const float4*>(fc + 12 + 4 * lane);
-          const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w,
-                               r4.x, r4.y, r4.z, r4.w};
+          // j and k neighbours straight from the 16-bit centre tile: the
+          // pair terms run in units of the centre plane's scale (the words
+          // themselves, 2u and the i-pair sums multiplied by the inverse
+          // scale) and the sum is scaled once; power-of-two scaling commutes
+          // with every rounding, so this is bit for bit the scaled sum.
+          const float inv1 = exp2i(-si.e_uc);
+          const uint16_t* row = uc + kKH16 + 4 * lane;
+          const uint2 wl = *reinterpret_cast<const uint2*>(row - 4);
+          const uint2 wc = *reinterpret_cast<const uint2*>(row);
+          const uint2 wr = *reinterpret_cast<const uint2*>(row + 4);
+          const P4 l4 = words4<KIND>(wl);
+          const P4 c4 = words4<KIND>(wc);
+          const P4 r4 = words4<KIND>(wr);
+          const float w[12] = {l4.a.x, l4.a.y, l4.b.x, l4.b.y, c4.a.x, c4.a.y, c4.b.x, c4.b.y,
+                               r4.a.x, r4.a.y, r4.b.x, r4.b.y};
           // centre values: the word, plus the low byte in the compensated form
-          P4 u0 = {make_float2(c4.x, c4.y), make_float2(c4.z, c4.w)};
+          P4 u0 = mul4(c4, sc);
           if (HILO) {
-            const uint2 cw = *reinterpret_cast<const uint2*>(uc + kKH16 + 4 * lane);
             const uint32_t lb = *reinterpret_cast<const uint32_t*>(ulr + stage * LSLOT + r * kTK + 4 * lane);
-            const uint16_t cb[4] = {(uint16_t)(cw.x & 0xffff), (uint16_t)(cw.x >> 16),
-                                    (uint16_t)(cw.y & 0xffff), (uint16_t)(cw.y >> 16)};
+            const uint16_t cb[4] = {(uint16_t)(wc.x & 0xffff), (uint16_t)(wc.x >> 16),
+                                    (uint16_t)(wc.y & 0xffff), (uint16_t)(wc.y >> 16)};
             float uc4[4];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
@@ -352,29 +348,34 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
             u0 = {make_float2(uc4[0], uc4[1]), make_float2(uc4[2], uc4[3])};
           }
           const P4 u2 = add4(u0, u0);
-          const P4 nu2 = {make_float2(-u2.a.x, -u2.a.y), make_float2(-u2.b.x, -u2.b.y)};
+          const float2 ninv = make_float2(-inv1, -inv1);
+          const P4 nu2 = mul4(u2, ninv);  // -2u in the centre plane's units
           P4 acc;
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
             const int ax = pair_axis(P, p);
             const int rr = pair_r(P, p);
-            P4 av, bv;
-            if (ax == 2) {
-              av = {make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])};
-              bv = {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])};
+            P4 sum;
+            if (ax == 2 && (rr & 1)) {
+              // odd offsets straddle register pairs: one point at a time
+              sum = {make_float2(w[4 - rr] + w[4 + rr], w[5 - rr] + w[5 + rr]),
+                     make_float2(w[6 - rr] + w[6 + rr], w[7 - rr] + w[7 + rr])};
+            } else if (ax == 2) {
+              sum = add4({make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])},
+                         {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])});
             } else if (ax == 1) {
-              const float4 A = *reinterpret_cast<const float4*>(fc - rr * kUKW16 + kKH16 + 4 * lane);
-              const float4 B = *reinterpret_cast<const float4*>(fc + rr * kUKW16 + kKH16 + 4 * lane);
-              av = {make_float2(A.x, A.y), make_float2(A.z, A.w)};
-              bv = {make_float2(B.x, B.y), make_float2(B.z, B.w)};
+              const uint2 A = *reinterpret_cast<const uint2*>(row - rr * kUKW16);
+              const uint2 B = *reinterpret_cast<const uint2*>(row + rr * kUKW16);
+              sum = add4(words4<KIND>(A), words4<KIND>(B));
             } else {
-              av = q[(ph + 2 * QN - R - rr) % QN];
-              bv = q[(ph + QN - R + rr) % QN];
+              sum = mul4(add4(q[(ph + 2 * QN - R - rr) % QN], q[(ph + QN - R + rr) % QN]),
+                         make_float2(inv1, inv1));
             }
-            const P4 d = add4(add4(av, bv), nu2);
+            const P4 d = add4(sum, nu2);
             const float2 cf2 = make_float2(a.cf.cf[p], a.cf.cf[p]);
             acc = p == 0 ? mul4(d, cf2) : fma4(cf2, d, acc);
           }
+          acc = mul4(acc, sc);
           // v and s of plane i
           const uint2 vw = *reinterpret_cast<const uint2*>(vr + stage * VSLOT + (r * kTK + 4 * lane) * 2);
           const uint2 sw = *reinterpret_cast<const uint2*>(sr + stage * VSLOT + (r * kTK + 4 * lane) * 2);
@@ -475,7 +476,7 @@ size_t tma16_smem_bytes(int tj, int nv, int R, bool hilo) {
   const size_t vslot = (size_t)kTK * tj * 2;
   const size_t lslot = (size_t)kTK * tj;
   return (size_t)(nv + R) * uslot + 2 * (size_t)nv * vslot + (hilo ? 2 * (size_t)nv * lslot : 0) +
-         2 * (size_t)kFTile * 4 + 2 * (size_t)nv * 8 + (size_t)nv * sizeof(StageInfo) +
+         2 * (size_t)nv * 8 + (size_t)nv * sizeof(StageInfo) +
          2 * (size_t)nv * 4 + 128;
 }
 
@@ -505,6 +506,7 @@ cudaError_t launch16_p(const Tma16Plan& pl, const Tma16Args& args, const CUtenso
     case 4: return launch16_nv<KIND, HILO, P, 4>(pl, args, maps, stream, occupancy_out);
     case 6: return launch16_nv<KIND, HILO, P, 6>(pl, args, maps, stream, occupancy_out);
     case 8: return launch16_nv<KIND, HILO, P, 8>(pl, args, maps, stream, occupancy_out);
+    case 12: return launch16_nv<KIND, HILO, P, 12>(pl, args, maps, stream, occupancy_out);
     default: return cudaErrorInvalidConfiguration;
   }
 }
