@@ -29,7 +29,7 @@ namespace st3d {
 namespace {
 
 constexpr int kBTJ = 16;
-constexpr int kBNV = 3;
+constexpr int kBNV = 4;  // 4 stages: 241.5 against 237.8 Gpts/s with 3 on the 64-grid batch
 constexpr int kBRmax = 4;
 
 struct BatchGrid {
