@@ -458,11 +458,20 @@ def run_gb300(args, dist):
         # the plain kernel in FP64, 32 algorithmic bytes per point
         gp, msd, dinfo = time_storage(S, args.workload, "f64", args.fp64_steps, min(args.warmup, 3))
         ach = dinfo.bytes_per_point * pts / (msd * 1e-3) / 1e9
+        # FP64 arithmetic per point of the wave update: 3 per neighbour pair
+        # ((a+b), -2u, fma) plus 2u, -v and two fma; each one FP64-pipe
+        # instruction, against the nominal 1.25 TFLOP/s = 0.625 T FP64 fma/s
+        npairs = {7: 3, 13: 6, 25: 12}[points]
+        dp_ops = 3 * npairs + 4
+        dp_rate = dp_ops * pts / (msd * 1e-3) / 1e12
         result["fp64"] = {"value": dist.world * gp * (ms / ms_max), "unit": "Gpts/s",
                           "ms_per_step": msd, "bytes_per_point": dinfo.bytes_per_point,
                           "gflops": pts * dinfo.flops_per_point / (msd * 1e-3) / 1e9,
-                          "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
-                                       "frac": ach / peak},
+                          "roofline": {"bound": "fp64", "achieved": dp_rate, "peak": 0.625,
+                                       "unit": "T fp64 instr/s", "frac": dp_rate / 0.625,
+                                       "peak_kind": "nominal (1.25 TFLOP/s FP64)",
+                                       "fp64_ops_per_point": dp_ops,
+                                       "hbm_frac": ach / peak},
                           "kernel": "k_simple<double,%d,wave>" % points}
     if dist.rank == 0 and args.accuracy_steps > 0:
         acc = accuracy_run(S, args.workload, args.accuracy_steps, args.kernel, ["f32"] + forms)
