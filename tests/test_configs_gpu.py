@@ -1,0 +1,87 @@
+"""Parity at the benchmark configurations' full sizes.
+
+  - 7 points, 256^3, 20 steps and 25 points, 528^3, 200 steps, mode R on
+    seeded u, v ~ U[-1, 1), s ~ U[0.5, 1.5): the library through the drop-in
+    call equals the oracle's fused flavour bit for bit, and the reference
+    order (the oracle's plain flavour, pinned to the compiled reference)
+    within 1e-5 relative L2;
+  - 13 points, 1040^3, leapfrog wave with 8 seeded Gaussian blobs: two steps
+    fused per pass equal plain steps bit for bit (device-side difference);
+  - the 64-grid batch (axes U{64..320}, orders {7, 13, 25}): the graph
+    schedule equals the sequential one bit for bit on every grid.
+"""
+import numpy as np
+import pytest
+
+import stencil3d_gb300 as S
+from oracle import oracle as O
+from tests.helpers import mode_r_inputs, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("points,n,steps", [(7, 256, 20), (25, 528, 200)])
+def test_mode_r_full_size(points, n, steps):
+    grid = (n, n, n, 4, 4, 16)
+    v, s, u = mode_r_inputs(grid, 20251203 + points, "f32")
+    vg = v.copy()
+    with S.Stencil(S.Grid(*grid), points, "ref", "f32") as st:
+        assert st.info().kernel == S.KERNEL_TMA
+        st.iterate_host(vg, s, u, steps)
+    vf = v.copy()
+    O.iterate_ref(vf, s, u, grid, points, steps, fma=True)
+    np.testing.assert_array_equal(O.interior(vg, grid), O.interior(vf, grid))
+    if n <= 256:
+        vp = v.copy()
+        O.iterate_ref(vp, s, u, grid, points, steps, fma=False)
+        assert rel_l2(O.interior(vg, grid), O.interior(vp, grid)) <= 1e-5
+
+
+def test_temporal_blocking_full_size():
+    g = S.Grid(1040, 1040, 1040, 4, 4, 4)
+    ctx = []
+    try:
+        for T in (1, 2):
+            st = S.Stencil(g, 13, "wave", "f32", kernel="tma", temporal_block=T, dt=5e-4,
+                           src=(520, 520, 520))
+            ctx.append(st)
+            st.fill(S.FIELD_U, S.FILL_BLOBS, 20251203, 8, 20.0)
+            st.fill(S.FIELD_V, S.FILL_BLOBS, 20251203, 8, 20.0)
+            st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
+            st.iterate(21)
+            st.synchronize()
+        for field in (S.FIELD_U, S.FIELD_V):
+            d2, b2, dm, bm = ctx[1].norms(field, ctx[0], field)
+            assert b2 > 0 and d2 == 0.0 and dm == 0.0
+    finally:
+        for st in ctx:
+            st.close()
+
+
+def test_batch_full_workload_graph_equals_sequential():
+    import bench
+    specs = bench.batch_specs()
+    grids = [S.Grid(xs, ys, zs, 4, 4, 4) for (xs, ys, zs), _, _ in specs]
+    pts = [p for _, p, _ in specs]
+    dts = [1e-3 if p == 7 else 5e-4 for p in pts]
+    srcs = [sp for _, _, sp in specs]
+    batches = []
+    try:
+        for schedule in ("sequential", "graph"):
+            b = S.Batch(grids, pts, dt=dts, srcs=srcs)
+            batches.append(b)
+            for i in range(len(grids)):
+                st = b.context(i)
+                st.fill(S.FIELD_U, S.FILL_BLOBS, 7 + i, 4, 12.0)
+                st.fill(S.FIELD_V, S.FILL_BLOBS, 7 + i, 4, 12.0)
+                st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
+            b.iterate(5, schedule)
+            b.synchronize()
+        for i in range(len(grids)):
+            a, c = batches[0].context(i), batches[1].context(i)
+            for field in (S.FIELD_U, S.FIELD_V):
+                d2, b2, dm, bm = c.norms(field, a, field)
+                assert b2 > 0 and d2 == 0.0, (i, field)
+    finally:
+        for b in batches:
+            b.close()
