@@ -216,6 +216,19 @@ def ref_lib(points, dtype=np.float32):
     return L
 
 
+def ref_vec16_13():
+    """The reference's 13-point vec_16 kernel build (K = 6.25), or None."""
+    path = os.path.join(_build.REF_DIR, "libref13vec16.so")
+    if not os.path.exists(path):
+        return None
+    try:
+        L = C.CDLL(path)
+    except OSError:
+        return None
+    L.ref_iterate.argtypes = [_f32p, _f32p, _f32p] + [C.c_uint] * 7
+    return L
+
+
 def ref_iterate(v, s, u, grid, points, iterations, traversal="2d_jk_blocked"):
     """The reference's ITERATE (iterate_2d_jk_blocked, or iterate_3d) in place."""
     L = ref_lib(points, v.dtype)

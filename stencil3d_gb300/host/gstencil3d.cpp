@@ -9,7 +9,8 @@
 //
 // Added flags: --stencil N (2, 7, 13, 25; default 7 as config.h:38),
 // --wave (the leapfrog form, README.md:11-20, with --vel/--dt/--dx),
-// --kernel simple|tma|auto.
+// --kernel simple|tma|auto, --variant ref|vec8|vec16 (the reference's
+// compile-time kernel variant whose results to reproduce).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -47,6 +48,7 @@ int main(int argc, char** argv) {
   unsigned points = 7;
   real sbm = 12;
   const char* kernel = "auto";
+  const char* variant = "ref";
   gb300_options gopt;
 
   int iarg = 1;
@@ -74,6 +76,7 @@ int main(int argc, char** argv) {
     args += get_double_arg(argv, iarg, argc, "--dt", gopt.dt, 1e-9, 1.0);
     args += get_double_arg(argv, iarg, argc, "--dx", gopt.dx, 1e-6, 1e6);
     args += get_str_arg(argv, iarg, argc, "--kernel", kernel);
+    args += get_str_arg(argv, iarg, argc, "--variant", variant);
     if (args > 0) {
       iarg += args;
     } else {
@@ -94,6 +97,14 @@ int main(int argc, char** argv) {
     fprintf(stderr, "--zh must be larger or equal to %u for the %u-point stencil\n", radius, points);
     exit(2);
   }
+  // --variant names the reference's compile-time SUBTYPE/VLEN kernel whose
+  // results to reproduce: all have the ref kernel's arithmetic except the
+  // 13-point vec_16 kernel, whose K is 6.25 (stencil_13.h:391, 428)
+  if (strcmp(variant, "ref") != 0 && strcmp(variant, "vec16") != 0 && strcmp(variant, "vec8") != 0) {
+    fprintf(stderr, "--variant must be ref, vec8 or vec16\n");
+    return 2;
+  }
+  if (points == 13 && strcmp(variant, "vec16") == 0 && !wave) gopt.K = 6.25;
   gopt.points = (int)points;
   gopt.mode = wave ? ST3D_MODE_WAVE : ST3D_MODE_REF;
   gopt.kernel = strcmp(kernel, "simple") == 0 ? ST3D_KERNEL_SIMPLE

@@ -46,6 +46,10 @@ struct gb300_options {
   int storage = ST3D_F32;         // float; USE_DOUBLE -> ST3D_F64
   int kernel = ST3D_KERNEL_AUTO;
   double vel = 1500.0, dt = 1e-3, dx = 10.0;  // mode W physics
+  // Mode R diagonal coefficient K; 0 keeps the stencil's default.  The
+  // reference's 13-point vec_16 kernel uses 6.25 (stencil_13.h:391, 428)
+  // where every other 13-point kernel uses 3.5.
+  double K = 0.0;
 };
 
 // Per-call timing of the last iterate_gb300 call.

@@ -79,3 +79,17 @@ def test_wave_form_through_the_driver():
                        "--stencil", "25", "--wave", "--dt", "0.0005")
     assert rc == 0, err
     assert "leapfrog wave" in out and "finish compute in" in out
+
+
+@pytest.mark.gpu
+def test_vec16_variant_reproduces_the_reference_check():
+    """--variant vec16 gives the 13-point kernel the reference's vec_16 K =
+    6.25, whose known-answer check fails on every point (a step of -1.75
+    instead of +1), as the reference's vec_16 build reports."""
+    rc, out, err = run(CLI, "--xs", "16", "--ys", "16", "--zs", "32", "--iter", "2",
+                       "--stencil", "13", "--variant", "vec16")
+    assert rc == 0, err
+    assert out.count("check: 8192 errors found") == 2
+    rc, out, err = run(CLI, "--xs", "16", "--ys", "16", "--zs", "32", "--iter", "2",
+                       "--stencil", "13", "--variant", "ref")
+    assert rc == 0 and out.count("check: 0 errors found") == 2

@@ -266,3 +266,21 @@ def test_delta_form_scales_hold_a_source():
     uu, vv = O.delta_decode(fu, fd)
     assert np.all(np.isfinite(uu)) and np.all(np.isfinite(vv))
     assert np.max(np.abs(O.interior(uu, grid))) > 0
+
+
+def test_vec16_variant_is_ref_with_k_625():
+    """The reference's 13-point vec_16 kernel (stencil_13.h:359-430) computes
+    the ref kernel's update with K = 6.25 instead of 3.5: the oracle's plain
+    flavour with that K reproduces it bit for bit."""
+    L = O.ref_vec16_13()
+    if L is None:
+        pytest.skip("reference vec_16 build not available on this machine")
+    coefs = O.default_coefs(13, np.float32)
+    coefs[1] = 6.25
+    for grid in [(12, 16, 64, 4, 4, 16), (9, 13, 80, 4, 4, 16)]:
+        v, s, u = mode_r_inputs(grid, 5, "f32")
+        vr = v.copy()
+        L.ref_iterate(vr, s, u, *grid, 3)
+        vo = v.copy()
+        O.iterate_ref(vo, s, u, grid, 13, 3, coefs=coefs)
+        np.testing.assert_array_equal(O.interior(vr, grid), O.interior(vo, grid))

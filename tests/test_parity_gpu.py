@@ -201,3 +201,22 @@ def test_device_fill_matches_host_generator():
         st.download(v, u)
     np.testing.assert_array_equal(g.interior(u), O.interior(O.fill_uniform(grid, 42, 0, -1.0, 1.0), grid))
     assert np.all(g.interior(v) == 0.25)
+
+
+def test_vec16_variant_coefficient():
+    """Mode R with the 13-point vec_16 K = 6.25 (the reference's variant
+    kernel): bit-identical to the oracle's fused flavour with that K."""
+    grid = (20, 24, 130, 4, 4, 16)
+    v, s, u = mode_r_inputs(grid, 12, "f32")
+    o = S.default_opts(13, "ref", "f32")
+    o.coef[1] = 6.25
+    coefs = O.default_coefs(13, np.float32)
+    coefs[1] = 6.25
+    for kernel in (S.KERNEL_TMA, S.KERNEL_SIMPLE):
+        o.kernel = kernel
+        vv = v.copy()
+        with S.Stencil(S.Grid(*grid), 13, opts=o) as st:
+            st.iterate_host(vv, s, u, 4)
+        vf = v.copy()
+        O.iterate_ref(vf, s, u, grid, 13, 4, coefs=coefs, fma=True)
+        np.testing.assert_array_equal(O.interior(vv, grid), O.interior(vf, grid))
