@@ -345,12 +345,17 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
               sum = add4({w2_to_f2<KIND>(A.x), w2_to_f2<KIND>(A.y)},
                          {w2_to_f2<KIND>(B.x), w2_to_f2<KIND>(B.y)});
             } else {
-              sum = mul4(add4(q[(ph + 2 * QN - R - rr) % QN], q[(ph + QN - R + rr) % QN]),
-                         splat(si.inv_uc));
+              sum = add4(q[(ph + 2 * QN - R - rr) % QN], q[(ph + QN - R + rr) % QN]);
+              // the i pairs close the 13- and 25-point orders: the sum so far
+              // is scaled before the first of them, so they enter as they are;
+              // the 7-point order starts with its i pair, which enters in the
+              // centre plane's units
+              if (p == 0) sum = mul4(sum, splat(si.inv_uc));
+              else if (pair_axis(P, p - 1) != 0) acc = mul4(acc, splat(si.uc));
             }
             acc = p == 0 ? mul4(sum, splat(a.cf.cf[p])) : fma4(splat(a.cf.cf[p]), sum, acc);
           }
-          acc = mul4(acc, splat(si.uc));
+          if (pair_axis(P, NP - 1) != 0) acc = mul4(acc, splat(si.uc));
           const P4 lap = fma4(m2s, u0, acc);
           // d and s of plane i
           const uint2 dw = *reinterpret_cast<const uint2*>(dr + stage * VSLOT + (r * kTK + 4 * lane) * 2);

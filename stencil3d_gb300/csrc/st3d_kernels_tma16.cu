@@ -368,14 +368,24 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
               const uint2 B = *reinterpret_cast<const uint2*>(row + rr * kUKW16);
               sum = add4(words4<KIND>(A), words4<KIND>(B));
             } else {
-              sum = mul4(add4(q[(ph + 2 * QN - R - rr) % QN], q[(ph + QN - R + rr) % QN]),
-                         make_float2(inv1, inv1));
+              sum = add4(q[(ph + 2 * QN - R - rr) % QN], q[(ph + QN - R + rr) % QN]);
             }
-            const P4 d = add4(sum, nu2);
+            P4 d;
+            if (ax != 0) {
+              d = add4(sum, nu2);
+            } else if (p == 0) {
+              // the 7-point order starts with its i pair: centre plane units
+              d = add4(mul4(sum, make_float2(inv1, inv1)), nu2);
+            } else {
+              // the i pairs close the 13- and 25-point orders: the sum so far
+              // is scaled before the first of them and they enter as they are
+              if (pair_axis(P, p - 1) != 0) acc = mul4(acc, sc);
+              d = add4(sum, {make_float2(-u2.a.x, -u2.a.y), make_float2(-u2.b.x, -u2.b.y)});
+            }
             const float2 cf2 = make_float2(a.cf.cf[p], a.cf.cf[p]);
             acc = p == 0 ? mul4(d, cf2) : fma4(cf2, d, acc);
           }
-          acc = mul4(acc, sc);
+          if (pair_axis(P, NP - 1) != 0) acc = mul4(acc, sc);
           // v and s of plane i
           const uint2 vw = *reinterpret_cast<const uint2*>(vr + stage * VSLOT + (r * kTK + 4 * lane) * 2);
           const uint2 sw = *reinterpret_cast<const uint2*>(sr + stage * VSLOT + (r * kTK + 4 * lane) * 2);
