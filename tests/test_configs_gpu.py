@@ -85,3 +85,22 @@ def test_batch_full_workload_graph_equals_sequential():
     finally:
         for b in batches:
             b.close()
+
+
+@pytest.mark.parametrize("points", [7, 25])
+def test_largest_grid_the_reference_accepts(points):
+    """1264^3, the largest interior the reference's command line accepts
+    (main.cpp:125-144): 2.0e9 points, so linear indices run past 2^31.  The
+    known-answer run (u = s = 1, v = 0 gives v = n after n steps) holds on
+    every point, for the TMA and the direct-load kernels."""
+    g = S.Grid(1264, 1264, 1264, 4, 4, 16)
+    for kernel in ("tma", "simple"):
+        with S.Stencil(g, points, "ref", "f32", kernel=kernel) as st:
+            st.fill(S.FIELD_U, S.FILL_CONST, 0, 1.0)
+            st.fill(S.FIELD_S, S.FILL_CONST, 0, 1.0)
+            st.fill(S.FIELD_V, S.FILL_CONST, 0, 0.0)
+            st.iterate(2)
+            assert st.check(2.0) == 0
+            st.iterate(1)
+            assert st.check(3.0) == 0
+            assert st.check(2.0) == 1264 ** 3
