@@ -6,7 +6,7 @@
 //    counter hash for uniform noise, Gaussian blobs).
 //  - check: the reference's check() (iterators.cpp:304-325) as a count.
 //  - norms: sum (a-b)^2, sum b^2, max|a-b|, max|b| accumulated in double,
-//    the energy and L2 reductions that judge drift against an FP64 run.
+//    the energy and L2 reductions that measure drift against an FP64 run.
 //    Two passes with per-block partials in a scratch buffer and a fixed
 //    reduction order, so results are deterministic run to run.
 #include "st3d_f16.cuh"
