@@ -244,6 +244,27 @@ int st3d_norms_noalloc(const st3d_grid_desc* grid, const void* a, int storage_a,
 int st3d_timer_start(st3d_ctx* ctx);
 int st3d_timer_stop(st3d_ctx* ctx, float* ms);
 
+/* Summary of a context's run, the numbers the reference prints after its
+ * timed ITERATE (main.cpp:304-310): the last timer region (start to stop)
+ * with the steps taken inside it, its throughput, the reference's GFlop/s
+ * and memory-traffic figures for those steps (config.h:67-91 counts), the
+ * field energy sum(u^2) and max|u| of the current u (FP64), and, with a
+ * second context of the same interior, the relative L2 difference of u from
+ * that context's u (-1 without one). */
+typedef struct st3d_metrics {
+  uint64_t steps;          /* steps since the last upload (source clock) */
+  uint64_t timed_steps;    /* steps inside the last timer region */
+  double elapsed_ms;       /* the last timer region */
+  double gpts;             /* points x timed_steps / elapsed */
+  double gflops;           /* reference FLOPS_PER_STENCIL x points x timed_steps / elapsed */
+  double mem_gbs;          /* reference MEM_BYTES x points x timed_steps / elapsed */
+  double energy_u;         /* sum of u^2 over the interior */
+  double max_abs_u;        /* max |u| over the interior */
+  double rel_l2;           /* ||u - u_ref|| / ||u_ref||, or -1 */
+  double reserved[4];
+} st3d_metrics;
+int st3d_metrics_get(st3d_ctx* ctx, st3d_ctx* ref, st3d_metrics* out);
+
 /* Pinned host memory for fast upload/download. */
 int st3d_host_alloc(size_t bytes, void** ptr);
 int st3d_host_free(void* ptr);

@@ -64,6 +64,13 @@ class Info(C.Structure):
                 ("temporal_block", C.c_int32), ("host_path", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
+class Metrics(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("timed_steps", C.c_uint64), ("elapsed_ms", C.c_double),
+                ("gpts", C.c_double), ("gflops", C.c_double), ("mem_gbs", C.c_double),
+                ("energy_u", C.c_double), ("max_abs_u", C.c_double), ("rel_l2", C.c_double),
+                ("reserved", C.c_double * 4)]
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("grids", C.c_uint32), ("work_items", C.c_uint32), ("ctas", C.c_uint32),
                 ("graphs", C.c_uint32), ("interior_points", C.c_uint64), ("launches", C.c_uint64),
@@ -107,6 +114,7 @@ def lib():
             "st3d_norms": ([vp, i, vp, i, C.POINTER(C.c_double)], i),
             "st3d_timer_start": ([vp], i),
             "st3d_timer_stop": ([vp, C.POINTER(C.c_float)], i),
+            "st3d_metrics_get": ([vp, vp, C.POINTER(Metrics)], i),
             "st3d_host_alloc": ([C.c_size_t, C.POINTER(vp)], i),
             "st3d_host_free": ([vp], i),
             "st3d_ricker": ([C.c_double, C.c_double, C.c_double], C.c_double),
@@ -309,6 +317,14 @@ class Stencil:
         _ck(lib().st3d_norms(self._h, field, other._h if other is not None else None,
                              other_field, out))
         return tuple(out)
+
+    def metrics(self, ref=None):
+        """st3d_metrics_get: the last timer region's throughput and the
+        reference's GFlop/s and memory figures, energy and max of u, and the
+        relative L2 of u from `ref`'s u (-1 without)."""
+        m = Metrics()
+        _ck(lib().st3d_metrics_get(self._h, ref._h if ref is not None else None, C.byref(m)))
+        return {f: getattr(m, f) for f, _ in Metrics._fields_ if f != "reserved"}
 
     def rel_l2(self, other, field=FIELD_U, other_field=FIELD_U):
         d2, b2, dm, bm = self.norms(field, other, other_field)

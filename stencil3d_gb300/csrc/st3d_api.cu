@@ -1229,6 +1229,7 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
     c->vb = o1;
     c->ub = o2;
     c->step += T;
+    c->lvl += T;
     ++c->launches;
     iterations -= T;
   }
@@ -1442,6 +1443,7 @@ int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]) {
 int st3d_timer_start(st3d_ctx* c) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
   ST3D_CUDA(cudaEventRecord(c->ev0, c->stream));
+  c->timer_step0 = c->lvl;
   return ST3D_OK;
 }
 
@@ -1450,6 +1452,37 @@ int st3d_timer_stop(st3d_ctx* c, float* ms) {
   ST3D_CUDA(cudaEventRecord(c->ev1, c->stream));
   ST3D_CUDA(cudaEventSynchronize(c->ev1));
   ST3D_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev1));
+  c->timed_ms = *ms;
+  c->timed_steps = c->lvl - c->timer_step0;
+  return ST3D_OK;
+}
+
+int st3d_metrics_get(st3d_ctx* c, st3d_ctx* ref, st3d_metrics* m) {
+  if (!c || !m) return fail(ST3D_ERR_INVALID, "null argument");
+  memset(m, 0, sizeof *m);
+  m->steps = c->step;
+  m->timed_steps = c->timed_steps;
+  m->elapsed_ms = c->timed_ms;
+  const double pts = (double)c->grid.xs * c->grid.ys * c->grid.zs;
+  if (c->timed_ms > 0.0f && c->timed_steps > 0) {
+    const double per_s = pts * (double)c->timed_steps / (c->timed_ms * 1e-3);
+    const int P = c->opts.points;
+    const double flops = P == 2 ? 2 : P == 7 ? 12 : P == 13 ? 29 : 41;  // config.h:67-91
+    const double mem_reals = P == 2 ? 2 : 4;
+    m->gpts = per_s * 1e-9;
+    m->gflops = per_s * flops * 1e-9;
+    m->mem_gbs = per_s * mem_reals * host_elem_bytes(c->opts.storage) * 1e-9;
+  }
+  double out[4];
+  int rc = st3d_norms(c, ST3D_FIELD_U, nullptr, ST3D_FIELD_U, out);
+  if (rc != ST3D_OK) return rc;
+  m->energy_u = out[0];
+  m->max_abs_u = out[2];
+  m->rel_l2 = -1.0;
+  if (ref) {
+    if ((rc = st3d_norms(c, ST3D_FIELD_U, ref, ST3D_FIELD_U, out)) != ST3D_OK) return rc;
+    m->rel_l2 = out[1] > 0.0 ? sqrt(out[0] / out[1]) : sqrt(out[0]);
+  }
   return ST3D_OK;
 }
 

@@ -33,6 +33,9 @@ struct st3d_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = true;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  uint64_t timer_step0 = 0;    // steps at the last timer start
+  uint64_t timed_steps = 0;    // steps inside the last timer region
+  float timed_ms = 0.0f;
   uint64_t step = 0;
   uint64_t launches = 0;
   int kernel = ST3D_KERNEL_SIMPLE;

@@ -40,16 +40,18 @@ def test_struct_layout_matches_header(tmp_path):
     src = tmp_path / "sz.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "st3d.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(st3d_grid_desc),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(st3d_grid_desc),"
         " sizeof(st3d_opts), sizeof(st3d_info), offsetof(st3d_opts, c0),"
-        " offsetof(st3d_opts, src_f), offsetof(st3d_info, bytes_per_point)); return 0;}\n")
+        " offsetof(st3d_opts, src_f), offsetof(st3d_info, bytes_per_point),"
+        " sizeof(st3d_metrics)); return 0;}\n")
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)],
                    check=True)
     vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
                                            check=True).stdout.split()]
     assert vals == [C.sizeof(api.GridDesc), C.sizeof(api.Opts), C.sizeof(api.Info),
-                    api.Opts.c0.offset, api.Opts.src_f.offset, api.Info.bytes_per_point.offset]
+                    api.Opts.c0.offset, api.Opts.src_f.offset, api.Info.bytes_per_point.offset,
+                    C.sizeof(api.Metrics)]
 
 
 def test_abi_version_and_strings():

@@ -220,3 +220,29 @@ def test_vec16_variant_coefficient():
         vf = v.copy()
         O.iterate_ref(vf, s, u, grid, 13, 4, coefs=coefs, fma=True)
         np.testing.assert_array_equal(O.interior(vv, grid), O.interior(vf, grid))
+
+
+def test_metrics_report_the_timed_region():
+    """st3d_metrics_get: steps in the last timer region, throughput, the
+    reference's GFlop/s count, energy and max of u, relative L2 to another
+    context."""
+    grid = (20, 24, 140, 4, 4, 4)
+    g = S.Grid(*grid)
+    v, s, u = wave_inputs(grid, 8)
+    with S.Stencil(g, 13, "wave", "f32", dt=5e-4) as a, S.Stencil(g, 13, "wave", "f32", dt=5e-4) as b:
+        for st in (a, b):
+            st.upload(v, s, u)
+        a.iterate(2)
+        a.timer_start()
+        a.iterate(5)
+        a.timer_stop()
+        b.iterate(7)
+        m = a.metrics(b)
+        assert m["timed_steps"] == 5 and m["steps"] == 7 and m["elapsed_ms"] > 0
+        pts = 20 * 24 * 140
+        assert abs(m["gpts"] - pts * 5 / (m["elapsed_ms"] * 1e-3) / 1e9) < 1e-9 * m["gpts"] + 1e-12
+        assert abs(m["gflops"] - 29 * m["gpts"]) < 1e-9 * m["gflops"]
+        e2, _, em, _ = a.norms(S.FIELD_U)
+        assert m["energy_u"] == e2 and m["max_abs_u"] == em
+        assert m["rel_l2"] == 0.0
+        assert a.metrics()["rel_l2"] == -1.0
