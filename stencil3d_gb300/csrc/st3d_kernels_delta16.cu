@@ -34,6 +34,7 @@
 //     the scales of the next ones (the bound is in st3d_f16.cuh).
 #include "st3d_f16.cuh"
 #include "st3d_internal.h"
+#include "st3d_p4.cuh"
 #include "st3d_tma.cuh"
 
 namespace st3d {
@@ -75,42 +76,6 @@ struct Delta16Args {
   uint32_t* status;
 };
 
-struct P4 {
-  float2 a, b;
-};
-__device__ __forceinline__ P4 add4(const P4& x, const P4& y) {
-  return {__fadd2_rn(x.a, y.a), __fadd2_rn(x.b, y.b)};
-}
-__device__ __forceinline__ P4 mul4(const P4& x, float2 c) { return {__fmul2_rn(x.a, c), __fmul2_rn(x.b, c)}; }
-__device__ __forceinline__ P4 fma4(float2 c, const P4& x, const P4& y) {
-  return {__ffma2_rn(c, x.a, y.a), __ffma2_rn(c, x.b, y.b)};
-}
-__device__ __forceinline__ float2 splat(float x) { return make_float2(x, x); }
-
-template <int KIND>
-__device__ __forceinline__ float2 w2_to_f2(uint32_t w) {
-  if (KIND == 0) return __half22float2(*reinterpret_cast<const __half2*>(&w));
-  return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
-}
-template <int KIND>
-__device__ __forceinline__ uint32_t f2_to_w2(float2 x) {
-  if (KIND == 0) {
-    const __half2 h = __floats2half2_rn(x.x, x.y);
-    return *reinterpret_cast<const uint32_t*>(&h);
-  }
-  const __nv_bfloat162 h = __floats2bfloat162_rn(x.x, x.y);
-  return *reinterpret_cast<const uint32_t*>(&h);
-}
-// 4 words -> 4 floats times the plane scale (exact)
-template <int KIND>
-__device__ __forceinline__ P4 decode4(uint2 w, float sc) {
-  return {__fmul2_rn(w2_to_f2<KIND>(w.x), splat(sc)), __fmul2_rn(w2_to_f2<KIND>(w.y), splat(sc))};
-}
-// 4 floats -> 4 words at the plane scale 2^-e (inv = 2^-e)
-template <int KIND>
-__device__ __forceinline__ uint2 encode4(const P4& x, float inv) {
-  return make_uint2(f2_to_w2<KIND>(__fmul2_rn(x.a, splat(inv))), f2_to_w2<KIND>(__fmul2_rn(x.b, splat(inv))));
-}
 __device__ __forceinline__ float amax4(const P4& x, bool c0, bool c1, bool c2, bool c3, float m) {
   if (c0) m = fmaxf(m, fabsf(x.a.x));
   if (c1) m = fmaxf(m, fabsf(x.a.y));

@@ -27,6 +27,7 @@
 // the same operation order.
 #include "st3d_f16.cuh"
 #include "st3d_internal.h"
+#include "st3d_p4.cuh"
 #include "st3d_tma.cuh"
 
 namespace st3d {
@@ -85,46 +86,6 @@ struct Tma16Args {
 };
 
 __device__ __forceinline__ float mx(const uint32_t* M, int i) { return __uint_as_float(M[i]); }
-
-// 4 points as two float2 (packed FP32 pairs: __fadd2_rn / __ffma2_rn give
-// per component exactly __fadd_rn / __fmaf_rn).
-struct P4 {
-  float2 a, b;
-};
-__device__ __forceinline__ P4 add4(const P4& x, const P4& y) {
-  return {__fadd2_rn(x.a, y.a), __fadd2_rn(x.b, y.b)};
-}
-__device__ __forceinline__ P4 mul4(const P4& x, float2 c) { return {__fmul2_rn(x.a, c), __fmul2_rn(x.b, c)}; }
-__device__ __forceinline__ P4 fma4(float2 c, const P4& x, const P4& y) {
-  return {__ffma2_rn(c, x.a, y.a), __ffma2_rn(c, x.b, y.b)};
-}
-
-// 4 words -> 4 floats, unscaled
-template <int KIND>
-__device__ __forceinline__ P4 words4(uint2 w) {
-  if (KIND == 0)
-    return {__half22float2(*reinterpret_cast<const __half2*>(&w.x)),
-            __half22float2(*reinterpret_cast<const __half2*>(&w.y))};
-  return {__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w.x)),
-          __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w.y))};
-}
-
-template <int KIND>
-__device__ __forceinline__ P4 decode4(uint2 w, float2 sc) {
-  float2 lo, hi;
-  if (KIND == 0) {
-    lo = __half22float2(*reinterpret_cast<const __half2*>(&w.x));
-    hi = __half22float2(*reinterpret_cast<const __half2*>(&w.y));
-  } else {
-    lo = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w.x));
-    hi = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w.y));
-  }
-  return {__fmul2_rn(lo, sc), __fmul2_rn(hi, sc)};
-}
-
-__device__ __forceinline__ float p4c(const P4& x, int c) {
-  return c == 0 ? x.a.x : c == 1 ? x.a.y : c == 2 ? x.b.x : x.b.y;
-}
 
 template <int KIND, bool HILO, int P, int TJ, int NV>
 __global__ void __launch_bounds__((TJ + 1) * 32, 1)
@@ -309,7 +270,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
           const uint16_t* un = reinterpret_cast<const uint16_t*>(ur + (hh % NU) * USLOT) +
                                (r + R) * kUKW16 + kKH16 + 4 * lane;
           const float sc = exp2i(si.e_up);
-          q[ph] = decode4<KIND>(*reinterpret_cast<const uint2*>(un), make_float2(sc, sc));
+          q[ph] = decode4<KIND>(*reinterpret_cast<const uint2*>(un), sc);
         }
         float vmax = 0.0f;
         if (n >= 2 * R) {
@@ -402,9 +363,9 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
                                 W::to_float(vb[c])) * scv1;
             v0 = {make_float2(vv[0], vv[1]), make_float2(vv[2], vv[3])};
           } else {
-            v0 = decode4<KIND>(vw, make_float2(scv1, scv1));
+            v0 = decode4<KIND>(vw, scv1);
           }
-          P4 s0 = decode4<KIND>(sw, make_float2(scs1, scs1));
+          P4 s0 = decode4<KIND>(sw, scs1);
           if (i == a.src.i && j == a.src.j && (unsigned)(a.src.k - k) < 4u) {
             const int c = a.src.k - k;
             if (c == 0) s0.a.x = s0.a.x + a.src.amp;
