@@ -10,7 +10,9 @@
 // Added flags: --stencil N (2, 7, 13, 25; default 7 as config.h:38),
 // --wave (the leapfrog form, README.md:11-20, with --vel/--dt/--dx),
 // --kernel simple|tma|auto, --variant ref|vec8|vec16 (the reference's
-// compile-time kernel variant whose results to reproduce).
+// compile-time kernel variant whose results to reproduce), --storage
+// f32|f16|bf16|f16_hilo (device storage of the wave form) and
+// --temporal-block 1|2|4 (FP32 wave steps fused per pass).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -25,6 +27,18 @@ constexpr unsigned kDefaultSizeXY = 945;  // config.h:6
 constexpr unsigned kDefaultSizeZ = 880;   // config.h:7
 constexpr unsigned kDefaultOfs = 16;      // config.h:8
 constexpr unsigned kDefaultIter = 100;    // config.h:9
+
+// Zero every halo point of a field in the reference layout.
+void zero_halo(real* a, const s_grid& g) {
+  const long long ni = g.xsize + 2LL * g.xhalo, nj = g.ysize + 2LL * g.yhalo, nk = g.zsize + 2LL * g.zhalo;
+  for (long long i = 0; i < ni; ++i)
+    for (long long j = 0; j < nj; ++j)
+      for (long long k = 0; k < nk; ++k) {
+        const bool inner = i >= g.xhalo && i < g.xhalo + g.xsize && j >= g.yhalo &&
+                           j < g.yhalo + g.ysize && k >= g.zhalo && k < g.zhalo + g.zsize;
+        if (!inner) a[(i * nj + j) * nk + k] = 0.0f;
+      }
+}
 
 double flops_per_stencil(int points) {  // config.h:67-91
   return points == 2 ? 2 : points == 7 ? 12 : points == 13 ? 29 : 41;
@@ -49,6 +63,8 @@ int main(int argc, char** argv) {
   real sbm = 12;
   const char* kernel = "auto";
   const char* variant = "ref";
+  const char* storage = "f32";
+  unsigned tblock = 1;
   gb300_options gopt;
 
   int iarg = 1;
@@ -77,6 +93,8 @@ int main(int argc, char** argv) {
     args += get_double_arg(argv, iarg, argc, "--dx", gopt.dx, 1e-6, 1e6);
     args += get_str_arg(argv, iarg, argc, "--kernel", kernel);
     args += get_str_arg(argv, iarg, argc, "--variant", variant);
+    args += get_str_arg(argv, iarg, argc, "--storage", storage);
+    args += get_int_arg(argv, iarg, argc, "--temporal-block", tblock, 1, 4, 1);
     if (args > 0) {
       iarg += args;
     } else {
@@ -105,6 +123,20 @@ int main(int argc, char** argv) {
     return 2;
   }
   if (points == 13 && strcmp(variant, "vec16") == 0 && !wave) gopt.K = 6.25;
+  // host arrays are float (`real`): FP32 or one of the 16-bit device storages
+  if (strcmp(storage, "f32") == 0) gopt.storage = ST3D_F32;
+  else if (strcmp(storage, "f16") == 0) gopt.storage = ST3D_F16;
+  else if (strcmp(storage, "bf16") == 0) gopt.storage = ST3D_BF16;
+  else if (strcmp(storage, "f16_hilo") == 0) gopt.storage = ST3D_F16_HILO;
+  else {
+    fprintf(stderr, "--storage must be f32, f16, bf16 or f16_hilo\n");
+    return 2;
+  }
+  if (gopt.storage != ST3D_F32 && !wave) {
+    fprintf(stderr, "--storage %s needs --wave\n", storage);
+    return 2;
+  }
+  gopt.temporal_block = (int)tblock;
   gopt.points = (int)points;
   gopt.mode = wave ? ST3D_MODE_WAVE : ST3D_MODE_REF;
   gopt.kernel = strcmp(kernel, "simple") == 0 ? ST3D_KERNEL_SIMPLE
@@ -126,8 +158,8 @@ int main(int argc, char** argv) {
          grid.xsize, grid.ysize, grid.zsize, grid.xhalo, grid.yhalo, grid.zhalo,
          1e-9 * (double)grid.gsize * sizeof(real));
   printf(" -- using block tile size of %d x %d x %d\n", grid.xb_size, grid.yb_size, grid.zb_size);
-  printf(" -- GB300: %s form, %s kernel, one GPU\n", wave ? "leapfrog wave" : "reference",
-         kernel);
+  printf(" -- GB300: %s form, %s kernel, %s storage, %u step(s) per pass, one GPU\n",
+         wave ? "leapfrog wave" : "reference", kernel, storage, tblock);
 
   // pinned host arrays, shifted like main.cpp:272-275
   const size_t page = 1UL << 16;
@@ -145,6 +177,12 @@ int main(int argc, char** argv) {
   printf("[rank%i] Phase #%i: array initialization\n", my_rank, ++phase);
   double t0 = seconds();
   init_arrays(ov, os, ou, asize / sizeof(real));
+  // the 16-bit storages and fused steps hold a zero (Dirichlet) boundary
+  if (wave && (gopt.storage != ST3D_F32 || tblock > 1)) {
+    zero_halo(v, grid);
+    zero_halo(s, grid);
+    zero_halo(u, grid);
+  }
   double t1 = seconds();
   printf("[rank%i] Phase #%i: initialization took %f secs\n", my_rank, ++phase, t1 - t0);
 

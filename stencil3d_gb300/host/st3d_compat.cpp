@@ -31,6 +31,7 @@ st3d_ctx* context_for(const s_grid& g) {
   if (rc) die(rc, "st3d_default_opts");
   o.kernel = g_opts.kernel;
   if (g_opts.K != 0.0) o.coef[1] = g_opts.K;
+  o.temporal_block = g_opts.temporal_block;
   if (g_opts.mode == ST3D_MODE_WAVE) {
     rc = st3d_set_wave_physics(&o, g_opts.vel, g_opts.dt, g_opts.dx);
     if (rc) die(rc, "st3d_set_wave_physics");

@@ -50,6 +50,7 @@ struct gb300_options {
   // reference's 13-point vec_16 kernel uses 6.25 (stencil_13.h:391, 428)
   // where every other 13-point kernel uses 3.5.
   double K = 0.0;
+  int temporal_block = 1;         // mode W, FP32: steps fused per pass
 };
 
 // Per-call timing of the last iterate_gb300 call.

@@ -93,3 +93,22 @@ def test_vec16_variant_reproduces_the_reference_check():
     rc, out, err = run(CLI, "--xs", "16", "--ys", "16", "--zs", "32", "--iter", "2",
                        "--stencil", "13", "--variant", "ref")
     assert rc == 0 and out.count("check: 0 errors found") == 2
+
+
+def test_storage_needs_the_wave_form():
+    rc, out, err = run(CLI, "--storage", "f16")
+    assert rc == 2 and "--storage f16 needs --wave" in err
+    rc, out, err = run(CLI, "--wave", "--storage", "int8")
+    assert rc == 2 and "--storage must be" in err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("extra", [["--storage", "f16"], ["--storage", "f16_hilo"],
+                                   ["--stencil", "7", "--temporal-block", "4"]])
+def test_wave_forms_through_the_driver(extra):
+    args = ["--xs", "40", "--ys", "40", "--zs", "128", "--iter", "8", "--wave", "--dt", "0.0005"]
+    if "--stencil" not in extra:
+        args += ["--stencil", "25"]
+    rc, out, err = run(CLI, *(args + extra))
+    assert rc == 0, err
+    assert "leapfrog wave" in out and "finish compute in" in out
