@@ -249,6 +249,15 @@ def batch_run(S, steps, warmup):
                              "ms_per_step": ms / steps,
                              "launches": int(b.info().launches - l0)}
     out["graph_vs_sequential"] = out["graph"]["value"] / out["sequential"]["value"]
+    # the autotuner's pick of unit length and schedule for this batch
+    import tempfile
+    from stencil3d_gb300 import autotune
+    with tempfile.TemporaryDirectory() as tmp:
+        best = autotune.tune_batch(grids, pts, dts=dts, srcs=srcs, steps=20,
+                                   cache=os.path.join(tmp, "tune.json"))
+    out["tuned"] = {"opts": best["opts"], "value": best["gpts"], "unit": "Gpts/s",
+                    "table": [[c, None if ms is None else total / (ms * 1e-3) / 1e9]
+                              for c, ms in best["table"]]}
     return out
 
 

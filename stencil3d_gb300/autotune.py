@@ -2,6 +2,9 @@
 (grid, stencil order, mode, storage) by timing candidate configurations on the
 device, and keeps the choice in a JSON cache.
 
+For a batch of grids (``tune_batch``) the knobs are the planes per work
+unit and the schedule (CUDA graph or plain persistent launches).
+
 The knobs are the ``st3d_opts`` fields that change how the work is tiled,
 never what is computed: the kernel (TMA pipeline or plain), tile rows
 (``tile_j``), pipeline stages (``stages``), planes per work unit (``ichunk``)
@@ -137,6 +140,76 @@ def tune(grid, points, mode="wave", storage="f32", steps=10, cache=None, refresh
     result = {"key": key, "opts": best, "ms_per_step": ms, "gpts": pts / (ms * 1e-3) / 1e9,
               "table": table, "tuning_s": time.perf_counter() - t0}
     data = load_cache(path)  # another process may have added keys meanwhile
+    data[key] = result
+    save_cache(path, data)
+    return result
+
+
+def batch_key(grids, points, device=None):
+    """Cache key of a batch: device, and a digest of the (sizes, halos,
+    order) list in order."""
+    import hashlib
+    d = device if device is not None else api.device_info()
+    desc = ";".join("%dx%dx%d|%d,%d,%d|%d" % (g.xsize, g.ysize, g.zsize, g.xhalo, g.yhalo, g.zhalo, p)
+                    for g, p in zip(grids, points))
+    return "sm%d_cc%d%d|batch|%d|%s" % (d["sm_count"], d["cc"][0], d["cc"][1], len(grids),
+                                         hashlib.sha1(desc.encode()).hexdigest()[:16])
+
+
+def batch_candidates():
+    """Batch knobs: planes per work unit (shorter units balance the shared
+    queue, longer ones re-read fewer warm-up planes) and the schedule."""
+    return [{"ichunk": ic, "schedule": sch} for ic in (32, 64, 128) for sch in ("graph", "persistent")]
+
+
+def measure_batch_device(grids, points, cand, dts=None, srcs=None, steps=20, warmup=3):
+    """Milliseconds per step of a batch under one candidate (seeded blob
+    fields, CUDA events around `steps` steps)."""
+    try:
+        b = api.Batch(grids, points, dt=dts, srcs=srcs, ichunk=cand["ichunk"])
+    except api.St3dError:
+        return None
+    try:
+        for i in range(len(grids)):
+            st = b.context(i)
+            st.fill(api.FIELD_U, api.FILL_BLOBS, 1 + i, 4, 12.0)
+            st.fill(api.FIELD_V, api.FILL_BLOBS, 1 + i, 4, 12.0)
+            st.fill(api.FIELD_S, api.FILL_CONST, 0, 0.0)
+        b.iterate(warmup, cand["schedule"])
+        b.synchronize()
+        b.timer_start()
+        b.iterate(steps, cand["schedule"])
+        ms = b.timer_stop()
+        b.synchronize()
+        return ms / steps
+    except api.St3dError:
+        return None
+    finally:
+        b.close()
+
+
+def tune_batch(grids, points, dts=None, srcs=None, steps=20, cache=None, refresh=False,
+               measure=None, device=None):
+    """Best batch configuration: {"opts": {"ichunk", "schedule"}, "ms_per_step",
+    "gpts", "table", "key"}, cached like `tune`."""
+    path = cache if cache is not None else default_cache_path()
+    key = batch_key(grids, points, device)
+    data = load_cache(path)
+    if not refresh and key in data:
+        return data[key]
+    if measure is None:
+        def measure(c):
+            return measure_batch_device(grids, points, c, dts=dts, srcs=srcs, steps=steps)
+    t0 = time.perf_counter()
+    table = [[c, measure(c)] for c in batch_candidates()]
+    timed = [(c, ms) for c, ms in table if ms is not None and ms > 0]
+    if not timed:
+        raise api.St3dError(api.ERR_UNSUPPORTED, "no batch configuration ran")
+    best, ms = min(timed, key=lambda x: x[1])
+    pts = sum(g.xsize * g.ysize * g.zsize for g in grids)
+    result = {"key": key, "opts": best, "ms_per_step": ms, "gpts": pts / (ms * 1e-3) / 1e9,
+              "table": table, "tuning_s": time.perf_counter() - t0}
+    data = load_cache(path)
     data[key] = result
     save_cache(path, data)
     return result

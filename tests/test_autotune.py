@@ -75,3 +75,23 @@ def test_cache_survives_a_corrupt_file(tmp_path):
     r = autotune.tune(GRID, 7, "wave", "f32", cache=str(path), measure=lambda c: 1.0, device=DEV)
     assert r["opts"] == autotune.candidates(7, "wave", "f32")[0]
     assert json.load(open(path))[r["key"]]["ms_per_step"] == 1.0
+
+
+def test_tune_batch_picks_and_caches(tmp_path):
+    path = str(tmp_path / "tune.json")
+    grids = [S.Grid(64, 80, 96, 4, 4, 4), S.Grid(120, 64, 200, 4, 4, 4)]
+    pts = [7, 25]
+    seen = []
+
+    def model(c):
+        seen.append(c)
+        return {32: 3.0, 64: 2.0, 128: 2.5}[c["ichunk"]] - (0.1 if c["schedule"] == "graph" else 0.0)
+
+    r = autotune.tune_batch(grids, pts, cache=path, measure=model, device=DEV)
+    assert r["opts"] == {"ichunk": 64, "schedule": "graph"}
+    assert len(seen) == len(autotune.batch_candidates())
+    r2 = autotune.tune_batch(grids, pts, cache=path, measure=model, device=DEV)
+    assert r2["opts"] == r["opts"] and len(seen) == len(autotune.batch_candidates())
+    # a different batch has its own key
+    other = autotune.batch_key(grids[::-1], pts[::-1], DEV)
+    assert other != r["key"]

@@ -56,3 +56,11 @@ def test_tuner_end_to_end(tmp_path):
         info = st.info()
         if best["opts"].get("temporal_block", 1) > 1:
             assert info.temporal_block == best["opts"]["temporal_block"]
+
+
+def test_batch_tuner_end_to_end(tmp_path):
+    grids = [S.Grid(70, 90, 130, 4, 4, 4), S.Grid(100, 64, 200, 4, 4, 4), S.Grid(64, 64, 64, 4, 4, 4)]
+    pts = [7, 13, 25]
+    best = autotune.tune_batch(grids, pts, dts=[1e-3, 5e-4, 5e-4], steps=3,
+                               cache=str(tmp_path / "tune.json"))
+    assert best["gpts"] > 0 and best["opts"]["schedule"] in ("graph", "persistent")
