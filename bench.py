@@ -178,13 +178,22 @@ def init_fields(S, st, init):
     st.synchronize()
 
 
-def accuracy_run(S, wl, steps, kernel, storages):
+def accuracy_run(S, wl, steps, kernel, storages, guard_tol=1e-3):
     """Runs of the same workload in each storage next to an FP64 run; relative
     L2 and max error of u against FP64 every 100 steps (FP64 device
-    reductions)."""
+    reductions).  With guard_tol, also the guarded precision form: FP16 delta
+    storage that moves to the compensated form when its error against the
+    FP64 run passes guard_tol at a check (stencil3d_gb300.precision)."""
+    from stencil3d_gb300.precision import GuardedWave
+    points, xs, ys, zs, halo, dt, init = WORKLOADS[wl]
     ref_g, ref = make_stencil(S, wl, "f64")
     runs = {st: make_stencil(S, wl, st, kernel if st == "f32" else "auto")[1] for st in storages}
     report = {st: [] for st in storages}
+    guard = None
+    if guard_tol:
+        guard = GuardedWave(ref_g, points, tol=guard_tol, dt=dt, src=(xs // 2, ys // 2, zs // 2))
+        init_fields(S, guard, init)
+        guard_s = 0.0
     done = 0
     while done < steps:
         n = min(100, steps - done)
@@ -198,9 +207,24 @@ def accuracy_run(S, wl, steps, kernel, storages):
             d2, b2, dm, bm = runs[st].norms(S.FIELD_U, ref, S.FIELD_U)
             report[st].append({"step": done, "rel_l2": (d2 / b2) ** 0.5 if b2 > 0 else None,
                                "max_abs": dm, "rel_max": dm / bm if bm > 0 else None})
+        if guard is not None:
+            t0 = time.perf_counter()
+            guard.iterate(n)
+            guard.synchronize()
+            guard.check(ref)  # the move to the fallback, when it happens, is timed too
+            guard_s += time.perf_counter() - t0
     for r in runs.values():
         r.close()
     ref.close()
+    if guard is not None:
+        report["guarded"] = {
+            "tol": guard_tol, "storage": guard.storage, "fallback": guard.fallback,
+            "switched_at": guard.switched_at,
+            "value": xs * ys * zs * steps / guard_s / 1e9, "unit": "Gpts/s",
+            "value_note": "host wall clock per 100-step chunk, incl. the error check and the move",
+            "accuracy_vs_fp64": [{"step": st, "storage": sto, "rel_l2": e} for st, sto, e in guard.history],
+            "l2_err_vs_fp64": guard.history[-1][2] if guard.history else None}
+        guard.close()
     return report
 
 
@@ -483,8 +507,11 @@ def run_gb300(args, dist):
                                        "hbm_frac": ach / peak},
                           "kernel": "k_simple<double,%d,wave>" % points}
     if dist.rank == 0 and args.accuracy_steps > 0:
-        acc = accuracy_run(S, args.workload, args.accuracy_steps, args.kernel, ["f32"] + forms)
+        acc = accuracy_run(S, args.workload, args.accuracy_steps, args.kernel, ["f32"] + forms,
+                           guard_tol=1e-3 if "f16" in forms else 0)
         result["accuracy_vs_fp64"] = acc["f32"]
+        if "guarded" in acc:
+            result["fp16"]["f16_guarded"] = acc["guarded"]
         result["l2_err_fp32_vs_fp64"] = acc["f32"][-1]["rel_l2"]
         for form in forms:
             result["fp16"][form]["accuracy_vs_fp64"] = acc[form]

@@ -188,6 +188,10 @@ int st3d_destroy(st3d_ctx* ctx);
 int st3d_get_info(const st3d_ctx* ctx, st3d_info* info);
 /* The context's CUDA stream (a cudaStream_t), for callers that order work. */
 int st3d_get_stream(const st3d_ctx* ctx, void** stream);
+/* Set the mode W source clock (the step index the next step's Ricker
+ * amplitude is taken at; st3d_upload and st3d_fill reset it to 0), e.g. to
+ * continue a run in another context after moving its fields there. */
+int st3d_set_step(st3d_ctx* ctx, uint64_t step);
 
 /* Copy reference-layout host arrays in (NULL: leave that field): interior,
  * min(halo, 4) halo planes and rows, and the k halo (the stencil reads u's

@@ -114,6 +114,7 @@ def lib():
             "st3d_norms": ([vp, i, vp, i, C.POINTER(C.c_double)], i),
             "st3d_timer_start": ([vp], i),
             "st3d_timer_stop": ([vp, C.POINTER(C.c_float)], i),
+            "st3d_set_step": ([vp, C.c_uint64], i),
             "st3d_metrics_get": ([vp, vp, C.POINTER(Metrics)], i),
             "st3d_host_alloc": ([C.c_size_t, C.POINTER(vp)], i),
             "st3d_host_free": ([vp], i),
@@ -296,6 +297,10 @@ class Stencil:
 
     def iterate(self, iterations=1):
         _ck(lib().st3d_iterate(self._h, int(iterations)))
+
+    def set_step(self, step):
+        """The mode W source clock (reset to 0 by upload and fill)."""
+        _ck(lib().st3d_set_step(self._h, int(step)))
 
     def iterate_host(self, v, s, u, iterations):
         _ck(lib().st3d_iterate_host(self._h, _ptr(v, self.dtype), _ptr(s, self.dtype),

@@ -1114,6 +1114,12 @@ int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
   return ST3D_OK;
 }
 
+int st3d_set_step(st3d_ctx* c, uint64_t step) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  c->step = step;
+  return ST3D_OK;
+}
+
 int st3d_get_stream(const st3d_ctx* c, void** s) {
   if (!c || !s) return fail(ST3D_ERR_INVALID, "null argument");
   *s = (void*)c->stream;
