@@ -192,12 +192,23 @@ int st3d_get_stream(const st3d_ctx* ctx, void** stream);
  * amplitude is taken at; st3d_upload and st3d_fill reset it to 0), e.g. to
  * continue a run in another context after moving its fields there. */
 int st3d_set_step(st3d_ctx* ctx, uint64_t step);
+/* Move the time state of `src` into `dst` on the device: u and v as the
+ * values st3d_download returns, encoded in dst's storage, and the mode W step
+ * clock.  Both contexts on one device, same grid, same mode and the same host
+ * element type (FP32 for f32 and the 16-bit storages, FP64 for f64); s is not
+ * moved (set it in dst first: st3d_upload and st3d_fill reset the clock).
+ * dst's halo planes and rows become zero.  Allocates two device arrays of
+ * the reference layout for the duration of the call; synchronizes both
+ * streams.  Replaces a download into host arrays followed by an upload, e.g.
+ * to continue an FP16 run in the compensated storage. */
+int st3d_transfer(st3d_ctx* dst, st3d_ctx* src);
 
-/* Copy reference-layout host arrays in (NULL: leave that field): interior,
+/* Copy reference-layout arrays in (NULL: leave that field): interior,
  * min(halo, 4) halo planes and rows, and the k halo (the stencil reads u's
- * halo).  One contiguous host-to-device copy per field through a staging
- * buffer the context allocates on first use (the size of one host array).
- * Resets the mode W step clock to 0. */
+ * halo).  One contiguous copy per field through a staging buffer the context
+ * allocates on first use (the size of one host array).  The arrays may be
+ * host memory or device memory of the context's device (st3d_download
+ * likewise).  Resets the mode W step clock to 0. */
 int st3d_upload(st3d_ctx* ctx, const void* v, const void* s, const void* u);
 /* Copy interior points out: the host arrays' halo planes and rows are not
  * written, as the reference never writes halos; the k-halo points between

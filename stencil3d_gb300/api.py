@@ -115,6 +115,7 @@ def lib():
             "st3d_timer_start": ([vp], i),
             "st3d_timer_stop": ([vp, C.POINTER(C.c_float)], i),
             "st3d_set_step": ([vp, C.c_uint64], i),
+            "st3d_transfer": ([vp, vp], i),
             "st3d_metrics_get": ([vp, vp, C.POINTER(Metrics)], i),
             "st3d_host_alloc": ([C.c_size_t, C.POINTER(vp)], i),
             "st3d_host_free": ([vp], i),
@@ -301,6 +302,11 @@ class Stencil:
     def set_step(self, step):
         """The mode W source clock (reset to 0 by upload and fill)."""
         _ck(lib().st3d_set_step(self._h, int(step)))
+
+    def transfer_from(self, src):
+        """Take u, v and the step clock of `src` (same grid and mode) on the
+        device, encoded in this context's storage; s stays as it is."""
+        _ck(lib().st3d_transfer(self._h, src._h))
 
     def iterate_host(self, v, s, u, iterations):
         _ck(lib().st3d_iterate_host(self._h, _ptr(v, self.dtype), _ptr(s, self.dtype),

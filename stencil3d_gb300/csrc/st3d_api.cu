@@ -166,9 +166,9 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
   if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves the 7/13/25-point stencils");
   if (s16 && o->tile_j != 0 && o->tile_j != 16 &&
-      !(o->tile_j == 8 && (o->storage == ST3D_F16 || o->storage == ST3D_BF16)))
-    return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage runs 16-row tiles (8 also for FP16 / BF16), not %d",
-                o->tile_j);
+      !((o->tile_j == 8 || o->tile_j == 20) && (o->storage == ST3D_F16 || o->storage == ST3D_BF16)))
+    return fail(ST3D_ERR_UNSUPPORTED,
+                "16-bit storage runs 16-row tiles (8 or 20 also for FP16 / BF16), not %d", o->tile_j);
   if (o->temporal_block != 0 && o->temporal_block != 1 && o->temporal_block != 2 &&
       o->temporal_block != 4)
     return fail(ST3D_ERR_INVALID, "temporal blocking depth must be 1, 2 or 4 (got %d)",
@@ -331,10 +331,10 @@ int copy_field_strided(st3d_ctx* c, void* dev, void* host, bool to_device, bool 
   cudaPos dpos = make_cudaPos((c->L.pk - hz) * c->eb, c->L.pj - hy, c->L.pi - hx);
   if (to_device) {
     p.srcPtr = hp; p.srcPos = hpos; p.dstPtr = dp; p.dstPos = dpos;
-    p.kind = cudaMemcpyHostToDevice;
+    p.kind = cudaMemcpyDefault;
   } else {
     p.srcPtr = dp; p.srcPos = dpos; p.dstPtr = hp; p.dstPos = hpos;
-    p.kind = cudaMemcpyDeviceToHost;
+    p.kind = cudaMemcpyDefault;
   }
   p.extent = make_cudaExtent((g.zs + 2 * hz) * (size_t)hb, g.ys + 2 * hy, g.xs + 2 * hx);
   ST3D_CUDA(cudaMemcpy3DAsync(&p, c->stream));
@@ -382,7 +382,7 @@ int upload_field(st3d_ctx* c, void* dev, const void* host) {
   if (!src) {
     int rc = ensure_stage(c);
     if (rc != ST3D_OK) return rc;
-    ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyDefault, c->stream));
     src = c->stage;
     c->host_path = ST3D_HOST_STAGED;
   } else {
@@ -437,7 +437,7 @@ int download_field(st3d_ctx* c, const void* dev, void* host) {
   const size_t off = ((size_t)g.xh * R.imult + (size_t)g.yh * R.jmult) * hb;
   ST3D_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + off, R.imult * hb,
                               static_cast<const char*>(c->stage) + off, R.imult * hb,
-                              (size_t)g.ys * R.jmult * hb, g.xs, cudaMemcpyDeviceToHost, c->stream));
+                              (size_t)g.ys * R.jmult * hb, g.xs, cudaMemcpyDefault, c->stream));
   return ST3D_OK;
 }
 
@@ -475,10 +475,14 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
   const int R = c->R;
   const bool hilo = c->opts.storage == ST3D_F16_HILO;
   p->radius = R;
-  // The delta form also runs 8-row tiles, two CTAs per SM (on request; 16
-  // rows measured faster at 1024^3 for every order).
-  const int tj_want = c->opts.tile_j > 0 ? c->opts.tile_j : 16;
-  p->tj = (c->delta && tj_want == 8) ? 8 : 16;
+  // The delta form runs 16-, 20- or 8-row tiles (one CTA of 17 or 21 warps
+  // per SM, or two of 9).  Defaults measured at 1024^3 (FP16): 25 points 20
+  // rows x 10 stages 317 Gpts/s against 299 for 16 x 12; 7 points 20 x 8 545
+  // against 519; 13 points 16 x 8 459 against 357 for 20 x 8.
+  const int pts = c->opts.points;
+  const int tj_def = (c->delta && pts != 13) ? 20 : 16;
+  const int tj_want = c->opts.tile_j > 0 ? c->opts.tile_j : tj_def;
+  p->tj = (c->delta && (tj_want == 8 || tj_want == 20)) ? tj_want : 16;
   p->delta = c->delta;
   auto smem_of = [&](int nv) {
     return c->delta ? delta16_smem_bytes(p->tj, nv, R) : tma16_smem_bytes(p->tj, nv, R, hilo);
@@ -491,15 +495,27 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
                     : tma16_blocks_per_sm(c->opts.storage, c->opts.points, *p);
   };
   // the deepest pipeline that keeps the tile's CTAs per SM (two for 8 rows,
-  // one for 16); opts.stages may ask for one depth.  The delta form defaults
-  // to 12 stages for 25 points and 8 otherwise (measured at 1024^3: 25 points
-  // 248 -> 292 Gpts/s from 8 to 12 stages, 7 and 13 points flat or slower).
+  // one for 16 and 20); opts.stages may ask for one depth.  The delta form
+  // defaults to 12 stages for 25 points on 16 rows, 10 on 20 rows and 8
+  // otherwise (measured at 1024^3: 25 points on 16 rows 253 -> 299 Gpts/s
+  // from 8 to 12 stages, on 20 rows 270 / 296 / 317 at 6 / 8 / 10; 7 and 13
+  // points flat or slower past 8).
   const int want = c->opts.stages;
-  const int first = want ? want : c->delta ? (c->opts.points == 25 ? 12 : 8) : 12;
+  const int first = want ? want : !c->delta ? 12 : pts != 25 ? 8 : p->tj == 20 ? 10 : 12;
   const int need = p->tj == 8 ? 2 : 1;
+  // the depths the kernels are built for: 6/8/10 on 20 rows, 4/6/8/12 otherwise
+  auto built = [&](int nv) {
+    return p->tj == 20 ? (nv == 6 || nv == 8 || nv == 10) : (nv == 4 || nv == 6 || nv == 8 || nv == 12);
+  };
+  if (want && !built(want)) {
+    const int tj = p->tj;
+    delete p;
+    return fail(ST3D_ERR_UNSUPPORTED, "16-bit kernels on %d-row tiles run %s stages, not %d", tj,
+                tj == 20 ? "6, 8 or 10" : "4, 6, 8 or 12", want);
+  }
   int per_sm = 0;
-  for (int nv : {12, 8, 6, 4}) {
-    if (want ? nv != want : nv > first) continue;
+  for (int nv : {12, 10, 8, 6, 4}) {
+    if (!built(nv) || (want ? nv != want : nv > first)) continue;
     const int b = per_sm_of(nv);
     if (b >= need || (want && b >= 1)) {
       per_sm = b;
@@ -547,7 +563,7 @@ int upload_field16(st3d_ctx* c, int which, const void* host) {
   int rc = ensure_stage(c);
   if (rc != ST3D_OK) return rc;
   if (host)
-    ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    ST3D_CUDA(cudaMemcpyAsync(c->stage, host, host_array_bytes(c), cudaMemcpyDefault, c->stream));
   const st3d_grid_desc& g = c->grid;
   const RefGeom R = ref_geom(g);
   const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4, hz = (int)g.zh;
@@ -587,7 +603,7 @@ int download_field16(st3d_ctx* c, int which, void* host) {
   const size_t off = ((size_t)g.xh * R.imult + (size_t)g.yh * R.jmult) * 4;
   ST3D_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + off, R.imult * 4,
                               static_cast<const char*>(c->stage) + off, R.imult * 4,
-                              (size_t)g.ys * R.jmult * 4, g.xs, cudaMemcpyDeviceToHost, c->stream));
+                              (size_t)g.ys * R.jmult * 4, g.xs, cudaMemcpyDefault, c->stream));
   return ST3D_OK;
 }
 
@@ -699,7 +715,7 @@ int delta_download(st3d_ctx* c, void* host, bool v) {
   const size_t off = ((size_t)g.xh * R.imult + (size_t)g.yh * R.jmult) * 4;
   ST3D_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + off, R.imult * 4,
                               reinterpret_cast<const char*>(stage_slot(c, 0)) + off, R.imult * 4,
-                              (size_t)g.ys * R.jmult * 4, g.xs, cudaMemcpyDeviceToHost, c->stream));
+                              (size_t)g.ys * R.jmult * 4, g.xs, cudaMemcpyDefault, c->stream));
   return ST3D_OK;
 }
 
@@ -1120,6 +1136,42 @@ int st3d_set_step(st3d_ctx* c, uint64_t step) {
   return ST3D_OK;
 }
 
+int st3d_transfer(st3d_ctx* dst, st3d_ctx* src) {
+  if (!dst || !src) return fail(ST3D_ERR_INVALID, "null context");
+  if (dst == src) return fail(ST3D_ERR_INVALID, "transfer needs two contexts");
+  const st3d_grid_desc &a = dst->grid, &b = src->grid;
+  if (a.xs != b.xs || a.ys != b.ys || a.zs != b.zs || a.xh != b.xh || a.yh != b.yh || a.zh != b.zh)
+    return fail(ST3D_ERR_INVALID, "transfer between different grids");
+  if (dst->opts.mode != src->opts.mode) return fail(ST3D_ERR_INVALID, "transfer between different modes");
+  if (host_elem_bytes(dst->opts.storage) != host_elem_bytes(src->opts.storage))
+    return fail(ST3D_ERR_UNSUPPORTED, "transfer between FP64 and FP32-valued storages");
+  if (dst->device != src->device) return fail(ST3D_ERR_UNSUPPORTED, "transfer across devices");
+  if (!(src->has_u && src->has_v)) return fail(ST3D_ERR_STATE, "the source context holds no u and v");
+  const size_t bytes = host_array_bytes(src);
+  void* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, 2 * bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ST3D_ERR_NOMEM, "transfer buffers (%zu bytes): %s", 2 * bytes, cudaGetErrorString(e));
+  }
+  void* vb = buf;
+  void* ub = static_cast<char*>(buf) + bytes;
+  const uint64_t step = src->step;
+  int rc = ST3D_OK;
+  // zero halos; the download writes the interior rows with their k halo
+  e = cudaMemsetAsync(buf, 0, 2 * bytes, src->stream);
+  if (e != cudaSuccess) rc = cuda_fail(e, "transfer buffer clear");
+  if (rc == ST3D_OK) rc = st3d_download(src, vb, ub);  // synchronizes src's stream
+  if (rc == ST3D_OK) rc = st3d_upload(dst, vb, nullptr, ub);
+  if (rc == ST3D_OK) {
+    e = cudaStreamSynchronize(dst->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "transfer upload");
+  }
+  if (rc == ST3D_OK) dst->step = step;
+  cudaFree(buf);
+  return rc;
+}
+
 int st3d_get_stream(const st3d_ctx* c, void** s) {
   if (!c || !s) return fail(ST3D_ERR_INVALID, "null argument");
   *s = (void*)c->stream;
@@ -1136,10 +1188,10 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
       if (!(u && v) && !c->pair_valid && (rc = delta_rebuild_pair(c)) != ST3D_OK) return rc;
       c->pair_valid = false;
       if (u)
-        ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 0), u, host_array_bytes(c), cudaMemcpyHostToDevice,
+        ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 0), u, host_array_bytes(c), cudaMemcpyDefault,
                                   c->stream));
       if (v)
-        ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 1), v, host_array_bytes(c), cudaMemcpyHostToDevice,
+        ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 1), v, host_array_bytes(c), cudaMemcpyDefault,
                                   c->stream));
       if ((rc = delta_encode_pair(c, u != nullptr)) != ST3D_OK) return rc;
       if (u) c->has_u = true;
@@ -1147,7 +1199,7 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
     }
     if (s) {
       c->pair_valid = false;  // s passes through slot 0
-      ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 0), s, host_array_bytes(c), cudaMemcpyHostToDevice,
+      ST3D_CUDA(cudaMemcpyAsync(stage_slot(c, 0), s, host_array_bytes(c), cudaMemcpyDefault,
                                 c->stream));
       if ((rc = encode_staged16(c, stage_slot(c, 0), nullptr, c->fld[2], M_s(c), E_s(c), "s")) !=
           ST3D_OK)

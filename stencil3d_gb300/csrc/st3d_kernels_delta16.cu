@@ -18,9 +18,10 @@
 // ichunk-plane units, a producer warp streaming TMA tiles through an mbarrier
 // ring, one consumer warp per row, 4 points per lane, a register queue of
 // 2R+1 planes along i) with these differences:
-//   - the centre u tile is decoded to FP32 in shared memory once per step
-//     (each thread decodes 8 words; a named barrier publishes it), so that j
-//     and k neighbours are plain 128-bit FP32 loads;
+//   - the j and k neighbours are read as 16-bit words straight from the TMA
+//     tile (64-bit loads, four words per lane) and converted in registers;
+//     their sum runs in units of the centre plane's scale and is scaled once,
+//     so no decoded tile and no barrier between the consumer warps is needed;
 //   - lap = sum_p w_p (a_p + b_p) + m2s * u with m2s = -2 sum_p w_p, on
 //     packed FP32 pairs (fma.rn.f32x2 / add.rn.f32x2, per component exactly
 //     the scalar operations);
@@ -84,7 +85,8 @@ __device__ __forceinline__ float amax4(const P4& x, bool c0, bool c1, bool c2, b
   return m;
 }
 
-// TJ = 16 rows: one CTA of 17 warps per SM; TJ = 8: two CTAs of 9 warps.
+// TJ = 16 or 20 rows: one CTA of 17 or 21 warps per SM; TJ = 8: two CTAs of
+// 9 warps.
 template <int KIND, int P, int TJ, int NV>
 __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
     k_delta16(const __grid_constant__ CUtensorMap umap, const __grid_constant__ CUtensorMap dmap,
@@ -258,9 +260,10 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
         if (n >= nsteps) break;
         const uint32_t hh = h + (uint32_t)n;
         const int stage = (int)(hh % NV);
-        // After a timed-out wait the warp stops waiting but keeps stepping, so
-        // that every consumer warp reaches every named barrier below and the
-        // kernel ends (its results are then void; the status word says so).
+        // After a timed-out wait the warp stops waiting but keeps stepping and
+        // arriving on the stages' empty barriers, so that the producer's
+        // bounded waits end and the kernel returns (its results are then
+        // void; the status word says so).
         if (!failed && !mbar_wait_bounded(&full[stage], (hh / NV) & 1u, a.timeout_ns)) {
           atomicExch(a.status, (uint32_t)kDevTimeoutFull);
           failed = true;
@@ -410,9 +413,19 @@ cudaError_t launch_nv(const Tma16Plan& pl, const Delta16Args& args, const CUtens
   return cudaGetLastError();
 }
 
+// Pipeline depths per tile height: 8 and 16 rows take 4/6/8/12 stages; 20
+// rows (21 warps, 80 registers) take 6/8/10, the depths that fit 227 KB.
 template <int KIND, int P, int TJ>
 cudaError_t launch_tj(const Tma16Plan& pl, const Delta16Args& args, const CUtensorMap* maps,
                       cudaStream_t stream, int* occ) {
+  if (TJ == 20) {
+    switch (pl.nv) {
+      case 6: return launch_nv<KIND, P, TJ, 6>(pl, args, maps, stream, occ);
+      case 8: return launch_nv<KIND, P, TJ, 8>(pl, args, maps, stream, occ);
+      case 10: return launch_nv<KIND, P, TJ, 10>(pl, args, maps, stream, occ);
+      default: return cudaErrorInvalidConfiguration;
+    }
+  }
   switch (pl.nv) {
     case 4: return launch_nv<KIND, P, TJ, 4>(pl, args, maps, stream, occ);
     case 6: return launch_nv<KIND, P, TJ, 6>(pl, args, maps, stream, occ);
@@ -426,6 +439,7 @@ template <int KIND, int P>
 cudaError_t launch_p(const Tma16Plan& pl, const Delta16Args& args, const CUtensorMap* maps,
                      cudaStream_t stream, int* occ) {
   if (pl.tj == 16) return launch_tj<KIND, P, 16>(pl, args, maps, stream, occ);
+  if (pl.tj == 20) return launch_tj<KIND, P, 20>(pl, args, maps, stream, occ);
   if (pl.tj == 8) return launch_tj<KIND, P, 8>(pl, args, maps, stream, occ);
   return cudaErrorInvalidConfiguration;
 }

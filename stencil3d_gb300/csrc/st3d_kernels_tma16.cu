@@ -258,9 +258,10 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
         if (n >= nsteps) break;
         const uint32_t hh = h + (uint32_t)n;
         const int stage = (int)(hh % NV);
-        // After a timed-out wait the warp stops waiting but keeps stepping, so
-        // that every consumer warp reaches every named barrier below and the
-        // kernel ends (its results are then void; the status word says so).
+        // After a timed-out wait the warp stops waiting but keeps stepping and
+        // arriving on the stages' empty barriers, so that the producer's
+        // bounded waits end and the kernel returns (its results are then
+        // void; the status word says so).
         if (!failed && !mbar_wait_bounded(&full[stage], (hh / NV) & 1u, a.timeout_ns)) {
           atomicExch(a.status, (uint32_t)kDevTimeoutFull);
           failed = true;

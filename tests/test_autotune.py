@@ -45,9 +45,9 @@ def test_tune_picks_the_fastest_and_caches(tmp_path):
         return 10.0 - c.get("stages", 0) * 0.5 - (0.25 if c.get("tile_j") == 8 else 0.0)
 
     r = autotune.tune(GRID, 13, "wave", "f16", cache=path, measure=model, device=DEV)
-    assert r["opts"] == {"kernel": "tma", "tile_j": 8, "stages": 8}
-    assert abs(r["ms_per_step"] - 5.75) < 1e-12
-    assert r["gpts"] == pytest.approx(256 ** 3 / 5.75e-3 / 1e9)
+    assert r["opts"] == {"kernel": "tma", "tile_j": 20, "stages": 10}
+    assert abs(r["ms_per_step"] - 5.0) < 1e-12
+    assert r["gpts"] == pytest.approx(256 ** 3 / 5.0e-3 / 1e9)
     n = len(calls)
     assert n == len(autotune.candidates(13, "wave", "f16"))
     # cached: no measurement the second time

@@ -49,6 +49,26 @@ def test_f16_forms_match_oracle(storage, points, grid, blobs):
     np.testing.assert_array_equal(O.interior(vv, grid), O.interior(ov, grid))
 
 
+@pytest.mark.parametrize("points", [7, 25])
+@pytest.mark.parametrize("tile_j,stages", [(16, 12), (16, 4), (20, 10), (20, 6), (8, 8)])
+def test_delta_form_tiles_match_oracle(points, tile_j, stages):
+    """Every tile height and pipeline depth of the delta kernel gives the
+    oracle's bits; ys = 43 leaves a partial tile for 8, 16 and 20 rows."""
+    grid = (30, 43, 140, 4, 4, 4)
+    dt = 1e-3 if points == 7 else 5e-4
+    steps = 7
+    src = (15, 21, 70)
+    v, s, u = _inputs(grid, 40 + points, True)
+    with S.Stencil(S.Grid(*grid), points, "wave", "f16", dt=dt, src=src, tile_j=tile_j,
+                   stages=stages) as st:
+        assert st.info().tile_j == tile_j
+        uu, vv = u.copy(), v.copy()
+        st.iterate_host(vv, s, uu, steps)
+    ou, ov = _oracle_run("f16", u, v, s, grid, points, steps, dt, src)
+    np.testing.assert_array_equal(O.interior(uu, grid), O.interior(ou, grid))
+    np.testing.assert_array_equal(O.interior(vv, grid), O.interior(ov, grid))
+
+
 def _oracle_run(storage, u, v, s, grid, points, steps, dt, src=None, t0=0):
     """(u, v) after `steps` steps of the oracle's restatement of the form."""
     kind, hilo = O.storage_kind(storage)
