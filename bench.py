@@ -12,8 +12,9 @@ One step = one leapfrog time step over the whole grid (one kernel launch).
 ``value`` is whole-job throughput in Gpoints/s with the fields resident in
 HBM; ``e2e`` is the same metric through the drop-in C-ABI call
 ``st3d_iterate_host`` (ITERATE's replacement) on pinned host arrays, host
-to device and device to host copies inside the timed region.  Fields are
-13.4 GB, far larger than the 129 MB L2, so no flush is needed between steps.
+to device and device to host copies inside the timed region.  The u, v and
+s fields of the default workload take 13.9 GB in the device layout, far more
+than the 129 MB L2, so no flush is needed between steps.
 
 ``--impl reference`` times the CPU restatement of the path (the oracle; the
 reference's own compiled path where it runs on this machine) with every host
@@ -165,6 +166,13 @@ def make_stencil(S, wl, storage="f32", kernel="auto", temporal_block=1, **kw):
                    src=(xs // 2, ys // 2, zs // 2), temporal_block=temporal_block, **kw)
     init_fields(S, st, init)
     return g, st
+
+
+def l2_note(info):
+    """How the timed steps avoid L2 reuse: the u, v and s fields each step
+    streams are far larger than the 129 MB L2."""
+    fields = 3 * info.nk * info.nj * info.ni * 4 / 1e9
+    return "fields %.1f GB >> 129 MB L2, no flush needed" % fields
 
 
 def init_fields(S, st, init):
@@ -469,7 +477,7 @@ def run_gb300(args, dist):
                    "halo": halo, "form": "leapfrog wave", "dt": dt, "storage": "f32",
                    "kernel": kernel_tag, "tile_j": info.tile_j, "tile_k": info.tile_k,
                    "ichunk": info.ichunk,
-                   "l2": "fields 13.4 GB >> 129 MB L2, no flush needed",
+                   "l2": l2_note(info),
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
         "gflops": pts * args.steps * info.flops_per_point / (ms * 1e-3) / 1e9,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
