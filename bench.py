@@ -72,8 +72,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batch-steps", type=int, default=500,
                    help="steps of the batching-form run: 64 seeded grids (0 to skip)")
-    p.add_argument("--precision-forms", default="f16_hilo,f16,bf16",
+    p.add_argument("--precision-forms", default="f16_hilo,f16_hl,f16,bf16",
                    help="16-bit storage forms timed and judged against FP64 ('' to skip)")
+    p.add_argument("--guard-fallback", default="f16_hilo", choices=["f16_hilo", "f16_hl"],
+                   help="storage the guarded FP16 run moves to past half the tolerance")
     p.add_argument("--fp64-steps", type=int, default=5,
                    help="timed steps of the FP64 (USE_DOUBLE) run of the workload (0 to skip)")
     p.add_argument("--temporal-workloads", default="wave7_1024,wave13_1040",
@@ -186,7 +188,7 @@ def init_fields(S, st, init):
     st.synchronize()
 
 
-def accuracy_run(S, wl, steps, kernel, storages, guard_tol=1e-3):
+def accuracy_run(S, wl, steps, kernel, storages, guard_tol=1e-3, fallback="f16_hilo"):
     """Runs of the same workload in each storage next to an FP64 run; relative
     L2 and max error of u against FP64 every 100 steps (FP64 device
     reductions).  With guard_tol, also the guarded precision form: FP16 delta
@@ -199,7 +201,8 @@ def accuracy_run(S, wl, steps, kernel, storages, guard_tol=1e-3):
     report = {st: [] for st in storages}
     guard = None
     if guard_tol:
-        guard = GuardedWave(ref_g, points, tol=guard_tol, dt=dt, src=(xs // 2, ys // 2, zs // 2))
+        guard = GuardedWave(ref_g, points, tol=guard_tol, fallback=fallback, dt=dt,
+                            src=(xs // 2, ys // 2, zs // 2))
         init_fields(S, guard, init)
         guard_s = 0.0
     # The FP64 run advances in chunks of `every`: the guarded run is checked
@@ -525,7 +528,7 @@ def run_gb300(args, dist):
                           "kernel": "k_simple<double,%d,wave>" % points}
     if dist.rank == 0 and args.accuracy_steps > 0:
         acc = accuracy_run(S, args.workload, args.accuracy_steps, args.kernel, ["f32"] + forms,
-                           guard_tol=1e-3 if "f16" in forms else 0)
+                           guard_tol=1e-3 if "f16" in forms else 0, fallback=args.guard_fallback)
         result["accuracy_vs_fp64"] = acc["f32"]
         if "guarded" in acc:
             result["fp16"]["f16_guarded"] = acc["guarded"]

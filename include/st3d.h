@@ -74,7 +74,12 @@ typedef enum st3d_storage {
   /* u and v as FP16 words with a per-plane scale plus a signed byte per point
    * holding the rounding residual (~19 significant bits); 11 bytes per point
    * per step. */
-  ST3D_F16_HILO = 4
+  ST3D_F16_HILO = 4,
+  /* The delta form with u as an FP16 hi/lo pair: u = (hi + lo) * 2^E with
+   * lo = fp16(u * 2^-E - hi) (~22 significant bits), d one FP16 word; the
+   * stencil's neighbours are the hi words, the centre u the whole pair;
+   * 14 bytes per point per step. */
+  ST3D_F16_HL = 5
 } st3d_storage;
 
 typedef enum st3d_kernel {

@@ -260,8 +260,10 @@ def _lib16():
         L.orc16_iterate_wave.restype = C.c_int
         L.orc16_iterate_delta.argtypes = [
             C.c_int, _u16p, _i32p, _f32p, _u16p, _i32p, _f32p, _u16p, _i32p, _f32p, _u32p, C.c_int,
-            _f32p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_uint]
+            _f32p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_uint, C.c_void_p]
         L.orc16_iterate_delta.restype = C.c_int
+        L.orc16_encode_pair.argtypes = [_f32p, _u32p, _u16p, _u16p, _i32p, _f32p]
+        L.orc16_decode_pair.argtypes = [_u16p, _u16p, _i32p, _u32p, _f32p]
         L.orc16_scale_exponent.argtypes = [C.c_float]
         L.orc16_scale_exponent.restype = C.c_int
         L._f16_ready = True
@@ -289,9 +291,30 @@ class Field16:
         return x
 
 
+class FieldPair:
+    """A field in the FP16 hi/lo pair storage (the u of the F16_HL form):
+    words h and l with x = (h + l) * 2^E, per-plane scale exponents E and
+    maxima M."""
+
+    def __init__(self, x, grid):
+        self.kind, self.hilo, self.grid = 0, False, grid
+        self.h = np.zeros(shape(grid), np.uint16)
+        self.l = np.zeros(shape(grid), np.uint16)
+        self.E = np.zeros(grid[0], np.int32)
+        self.M = np.zeros(grid[0], np.float32)
+        _lib16().orc16_encode_pair(np.ascontiguousarray(x, np.float32), gvec(grid), self.h, self.l,
+                                   self.E, self.M)
+
+    def decode(self):
+        x = np.zeros(shape(self.grid), np.float32)
+        _lib16().orc16_decode_pair(self.h, self.l, self.E, gvec(self.grid), x)
+        return x
+
+
 def storage_kind(storage):
-    """(kind, hilo) of a 16-bit storage name."""
-    return {"f16": (0, False), "bf16": (1, False), "f16_hilo": (0, True)}[storage]
+    """(kind, hilo) of a 16-bit storage name (the F16_HL form is FP16 words
+    without the compensating byte)."""
+    return {"f16": (0, False), "bf16": (1, False), "f16_hilo": (0, True), "f16_hl": (0, False)}[storage]
 
 
 def k4_of(points, c1):
@@ -316,12 +339,14 @@ def iterate_wave16(u, v, s, grid, points, iterations, c1, c2, src=None, amps=Non
     return u, v
 
 
-def delta_fields(u, v, grid, kind):
-    """The FP16 / BF16 storage state of (u, v): Field16 of u and of the time
-    difference d = u - v (FP32 subtraction, as the library forms it)."""
+def delta_fields(u, v, grid, kind, pair=False):
+    """The FP16 / BF16 storage state of (u, v): Field16 of u (FieldPair with
+    `pair`, the F16_HL form) and of the time difference d = u - v (FP32
+    subtraction, as the library forms it)."""
     u = np.ascontiguousarray(u, np.float32)
     d = u - np.ascontiguousarray(v, np.float32)
-    return Field16(u, grid, kind, False), Field16(d, grid, kind, False)
+    fu = FieldPair(u, grid) if pair else Field16(u, grid, kind, False)
+    return fu, Field16(d, grid, kind, False)
 
 
 def delta_decode(fu, fd):
@@ -332,7 +357,7 @@ def delta_decode(fu, fd):
 
 def iterate_delta16(u, d, s, grid, points, iterations, c1, c2, src=None, amps=None, weights=None):
     """Mode W in the FP16 / BF16 delta form on Field16 states u, d (in place,
-    newest level afterwards) and s."""
+    newest level afterwards) and s; u a FieldPair runs the F16_HL form."""
     if weights is None:
         weights = wave_weights(points)
     srcv = None if src is None else np.asarray(src, dtype=np.int64)
@@ -341,6 +366,7 @@ def iterate_delta16(u, d, s, grid, points, iterations, c1, c2, src=None, amps=No
         u.kind, u.h, u.E, u.M, d.h, d.E, d.M, s.h, s.E, s.M, gvec(grid), points,
         np.ascontiguousarray(weights, np.float32), c1, c2, k4_of(points, c1),
         srcv.ctypes.data if srcv is not None else None,
-        ampv.ctypes.data if ampv is not None else None, iterations)
+        ampv.ctypes.data if ampv is not None else None, iterations,
+        u.l.ctypes.data if isinstance(u, FieldPair) else None)
     assert rc == 0, rc
     return u, d

@@ -597,6 +597,56 @@ void orc16_decode(int kind, int hilo, const uint16_t* h, const int8_t* q, const 
       }
 }
 
+/* FP16 hi/lo pair of a scaled value xs: h = f16(xs), l = f16(xs - h); the
+ * difference is exact in float, and h + l (exact in float: at most 22
+ * significant bits) is the decoded value. */
+static inline void enc_pair(float x, int E, uint16_t* h, uint16_t* l) {
+  const float xs = x * exp2i_f(-E);
+  *h = f32_to_f16(xs);
+  *l = f32_to_f16(xs - f16_to_f32(*h));
+}
+static inline float dec_pair(uint16_t h, uint16_t l, int E) {
+  return (f16_to_f32(h) + f16_to_f32(l)) * exp2i_f(E);
+}
+
+/* Encode a float field into the FP16 hi/lo pair storage (the u of the
+ * F16_HL form): plane maxima M, scales E (as orc16_encode), words h and l. */
+void orc16_encode_pair(const float* x, const unsigned* g, uint16_t* h, uint16_t* l, int* E,
+                       float* M) {
+  const orc_layout L = mk_layout(g);
+  for (unsigned i = 0; i < L.xs; i++) {
+    float m = 0.0f;
+    for (unsigned j = 0; j < L.ys; j++)
+      for (unsigned k = 0; k < L.zs; k++) {
+        const float a = fabsf(x[L.ijk_ofs + (size_t)i * L.imult + (size_t)j * L.jmult + k]);
+        if (a > m) m = a;
+      }
+    M[i] = m;
+    E[i] = orc16_scale_exponent(m);
+  }
+  const long long ni = L.xs + 2 * L.xh, nj = L.ys + 2 * L.yh, nk = L.zs + 2 * L.zh;
+  for (long long ii = 0; ii < ni; ii++) {
+    const long long i = ii - L.xh;
+    const int e = (i >= 0 && i < (long long)L.xs) ? E[i] : 0;
+    for (long long jj = 0; jj < nj; jj++)
+      for (long long kk = 0; kk < nk; kk++) {
+        const size_t p = (size_t)ii * L.imult + (size_t)jj * L.jmult + (size_t)kk;
+        enc_pair(x[p], e, &h[p], &l[p]);
+      }
+  }
+}
+
+void orc16_decode_pair(const uint16_t* h, const uint16_t* l, const int* E, const unsigned* g,
+                       float* x) {
+  const orc_layout L = mk_layout(g);
+  for (unsigned i = 0; i < L.xs; i++)
+    for (unsigned j = 0; j < L.ys; j++)
+      for (unsigned k = 0; k < L.zs; k++) {
+        const size_t p = L.ijk_ofs + (size_t)i * L.imult + (size_t)j * L.jmult + k;
+        x[p] = dec_pair(h[p], l[p], E[i]);
+      }
+}
+
 /* `iterations` steps; on return the u arrays hold U^{n+it} and the v arrays
  * U^{n+it-1} (contents swapped back after an odd count). */
 int orc16_iterate_wave(int kind, int hilo, uint16_t* uh, int8_t* uq, int* uE, float* uM,
@@ -712,11 +762,14 @@ int orc16_iterate_wave(int kind, int hilo, uint16_t* uh, int8_t* uq, int* uE, fl
  *            D'  = enc(d', Ed'),  u' = u + dec(D'),  U' = enc(u', Eu')
  *   maxima:  of |u'| and |d'| per plane.
  * u (uh, uE, uM) and d (dh, dE, dM) are updated in place to the newest
- * level. */
+ * level.  With ul (the F16_HL form, kind 0) u is the FP16 hi/lo pair
+ * (uh, ul): the centre value is dec_pair(uh, ul), the neighbours are the hi
+ * words alone, and u' is stored as a pair (enc_pair). */
 int orc16_iterate_delta(int kind, uint16_t* uh, int* uE, float* uM, uint16_t* dh, int* dE,
                         float* dM, const uint16_t* sh, const int* sE, const float* sM,
                         const unsigned* g, int points, const float* c, float c1, float c2,
-                        float k4, const long long* src, const float* amp, unsigned iterations) {
+                        float k4, const long long* src, const float* amp, unsigned iterations,
+                        uint16_t* ul) {
   const orc_layout L = mk_layout(g);
   const int R = radius_of(points);
   if (R < 0 || points == 2) return 1;
@@ -738,12 +791,13 @@ int orc16_iterate_delta(int kind, uint16_t* uh, int* uE, float* uM, uint16_t* dh
                                                 (size_t)src[1] * L.jmult + (size_t)src[2])
                                   : -1;
   uint16_t* u2 = (uint16_t*)calloc(L.gsize, sizeof(uint16_t));
+  uint16_t* l2 = ul ? (uint16_t*)calloc(L.gsize, sizeof(uint16_t)) : NULL;
   int* Ebuf = (int*)malloc(3 * (size_t)L.xs * sizeof(int));
   float* Mbuf = (float*)malloc(3 * (size_t)L.xs * sizeof(float));
-  if (!u2 || !Ebuf || !Mbuf) return 2;
+  if (!u2 || !Ebuf || !Mbuf || (ul && !l2)) return 2;
   int *UE = uE, *UE2 = Ebuf, *DEo = Ebuf + L.xs;
   float *UM = uM, *UM2 = Mbuf, *DMo = Mbuf + L.xs;
-  uint16_t *Uh = uh, *Uh2 = u2;
+  uint16_t *Uh = uh, *Uh2 = u2, *Ul = ul, *Ul2 = l2;
   for (unsigned it = 0; it < iterations; it++) {
     const float a = amp ? amp[it] : 0.0f;
     for (unsigned i = 0; i < L.xs; i++) {
@@ -774,7 +828,8 @@ int orc16_iterate_delta(int kind, uint16_t* uh, int* uE, float* uM, uint16_t* dh
                               w2f(kind, Uh[x + off_p[p]]) * exp2i_f(ep);
             acc = p == 0 ? cf[0] * sum : fmaf(cf[p], sum, acc);
           }
-          const float u0 = w2f(kind, Uh[x]) * exp2i_f(UE[i]);
+          /* the neighbours are the hi words; the centre is the whole pair */
+          const float u0 = Ul ? dec_pair(Uh[x], Ul[x], UE[i]) : w2f(kind, Uh[x]) * exp2i_f(UE[i]);
           const float lap = fmaf(m2s, u0, acc);
           const float d0 = w2f(kind, dh[x]) * exp2i_f(dE[i]);
           float s0 = w2f(kind, sh[x]) * exp2i_f(sE[i]);
@@ -783,7 +838,10 @@ int orc16_iterate_delta(int kind, uint16_t* uh, int* uE, float* uM, uint16_t* dh
           dh[x] = f2w(kind, dn * exp2i_f(-DEo[i]));
           const float dq = w2f(kind, dh[x]) * exp2i_f(DEo[i]);
           const float un = u0 + dq;
-          Uh2[x] = f2w(kind, un * exp2i_f(-UE2[i]));
+          if (Ul)
+            enc_pair(un, UE2[i], &Uh2[x], &Ul2[x]);
+          else
+            Uh2[x] = f2w(kind, un * exp2i_f(-UE2[i]));
           if (fabsf(un) > mu) mu = fabsf(un);
           if (fabsf(dn) > md) md = fabsf(dn);
         }
@@ -793,15 +851,18 @@ int orc16_iterate_delta(int kind, uint16_t* uh, int* uE, float* uM, uint16_t* dh
     memcpy(dE, DEo, L.xs * sizeof(int));
     memcpy(dM, DMo, L.xs * sizeof(float));
     { uint16_t* t = Uh; Uh = Uh2; Uh2 = t; }
+    { uint16_t* t = Ul; Ul = Ul2; Ul2 = t; }
     { int* t = UE; UE = UE2; UE2 = t; }
     { float* t = UM; UM = UM2; UM2 = t; }
   }
   if (Uh != uh) {
     memcpy(uh, Uh, L.gsize * sizeof(uint16_t));
+    if (ul) memcpy(ul, Ul, L.gsize * sizeof(uint16_t));
     memcpy(uE, UE, L.xs * sizeof(int));
     memcpy(uM, UM, L.xs * sizeof(float));
   }
   free(u2);
+  free(l2);
   free(Ebuf);
   free(Mbuf);
   return 0;

@@ -40,6 +40,11 @@ def candidates(points, mode, storage, zero_halo=False):
     """The configurations worth timing for one stencil/mode/storage, as
     dicts of ``st3d_opts`` overrides (0 = the library's automatic choice)."""
     out = []
+    if storage == "f16_hl":
+        for tj, depths in ((16, (4, 6, 8)), (20, (6, 8)), (8, (4, 6, 8))):
+            for nv in depths:
+                out.append({"kernel": "tma", "tile_j": tj, "stages": nv})
+        return out
     if storage in ("f16", "bf16"):
         for tj, depths in ((16, (4, 6, 8, 12)), (20, (6, 8, 10)), (8, (4, 6, 8, 12))):
             for nv in depths:

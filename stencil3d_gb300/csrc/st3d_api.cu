@@ -58,7 +58,8 @@ int elem_bytes(int storage) {
     case ST3D_F64: return 8;
     case ST3D_F16:
     case ST3D_BF16:
-    case ST3D_F16_HILO: return 2;
+    case ST3D_F16_HILO:
+    case ST3D_F16_HL: return 2;
     default: return 0;
   }
 }
@@ -69,9 +70,16 @@ int host_elem_bytes(int storage) { return storage == ST3D_F64 ? 8 : 4; }
 // (config.h:76,82,88 count these 4 streams); 2 points read u and write v
 // (config.h:70).  FP16 / BF16 delta form: read u, d, s and write u, d at 2
 // bytes each (10 B); the compensated form: 2-byte u, v, s and written v plus
-// the low bytes of the centre u, of v and of the written v (11 B).
+// the low bytes of the centre u, of v and of the written v (11 B); the delta
+// form with u as a hi/lo pair adds the lo words of the centre u, read and
+// written (14 B).
+// The word format of a 16-bit context's fields: the F16_HL form's words are
+// FP16 (its u carries a second word array of lo parts).
+int word_storage(int storage) { return storage == ST3D_F16_HL ? ST3D_F16 : storage; }
+
 double f16_bytes(int storage, int points, int eb) {
   if (storage == ST3D_F16_HILO) return 11.0;
+  if (storage == ST3D_F16_HL) return 14.0;
   if (storage == ST3D_F16 || storage == ST3D_BF16) return 10.0;
   return (points == 2 ? 2.0 : 4.0) * eb;
 }
@@ -154,7 +162,8 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_INVALID, "halo (%u,%u,%u) too wide", g->xh, g->yh, g->zh);
   if (o->mode == ST3D_MODE_WAVE && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the 2-point stencil has no wave form (it is not a Laplacian)");
-  const bool s16 = o->storage == ST3D_F16 || o->storage == ST3D_BF16 || o->storage == ST3D_F16_HILO;
+  const bool s16 = o->storage == ST3D_F16 || o->storage == ST3D_BF16 || o->storage == ST3D_F16_HILO ||
+                   o->storage == ST3D_F16_HL;
   if (s16 && o->mode != ST3D_MODE_WAVE)
     return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage is the precision form of the wave update only");
   if (s16 && o->kernel == ST3D_KERNEL_SIMPLE)
@@ -166,9 +175,9 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
   if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves the 7/13/25-point stencils");
   if (s16 && o->tile_j != 0 && o->tile_j != 16 &&
-      !((o->tile_j == 8 || o->tile_j == 20) && (o->storage == ST3D_F16 || o->storage == ST3D_BF16)))
+      !((o->tile_j == 8 || o->tile_j == 20) && o->storage != ST3D_F16_HILO))
     return fail(ST3D_ERR_UNSUPPORTED,
-                "16-bit storage runs 16-row tiles (8 or 20 also for FP16 / BF16), not %d", o->tile_j);
+                "16-bit storage runs 16-row tiles (8 or 20 also in the delta forms), not %d", o->tile_j);
   if (o->temporal_block != 0 && o->temporal_block != 1 && o->temporal_block != 2 &&
       o->temporal_block != 4)
     return fail(ST3D_ERR_INVALID, "temporal blocking depth must be 1, 2 or 4 (got %d)",
@@ -484,8 +493,9 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
   const int tj_want = c->opts.tile_j > 0 ? c->opts.tile_j : tj_def;
   p->tj = (c->delta && (tj_want == 8 || tj_want == 20)) ? tj_want : 16;
   p->delta = c->delta;
+  p->pair = c->pair;
   auto smem_of = [&](int nv) {
-    return c->delta ? delta16_smem_bytes(p->tj, nv, R) : tma16_smem_bytes(p->tj, nv, R, hilo);
+    return c->delta ? delta16_smem_bytes(p->tj, nv, R, c->pair) : tma16_smem_bytes(p->tj, nv, R, hilo);
   };
   auto per_sm_of = [&](int nv) {
     p->nv = nv;
@@ -503,15 +513,19 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
   const int want = c->opts.stages;
   const int first = want ? want : !c->delta ? 12 : pts != 25 ? 8 : p->tj == 20 ? 10 : 12;
   const int need = p->tj == 8 ? 2 : 1;
-  // the depths the kernels are built for: 6/8/10 on 20 rows, 4/6/8/12 otherwise
+  // the depths the kernels are built for: 6/8/10 on 20 rows, 4/6/8/12
+  // otherwise; the F16_HL form (a third tile per stage) 6/8 on 20 rows and
+  // 4/6/8 otherwise
   auto built = [&](int nv) {
+    if (c->pair) return p->tj == 20 ? (nv == 6 || nv == 8) : (nv == 4 || nv == 6 || nv == 8);
     return p->tj == 20 ? (nv == 6 || nv == 8 || nv == 10) : (nv == 4 || nv == 6 || nv == 8 || nv == 12);
   };
   if (want && !built(want)) {
     const int tj = p->tj;
     delete p;
     return fail(ST3D_ERR_UNSUPPORTED, "16-bit kernels on %d-row tiles run %s stages, not %d", tj,
-                tj == 20 ? "6, 8 or 10" : "4, 6, 8 or 12", want);
+                c->pair ? (tj == 20 ? "6 or 8" : "4, 6 or 8") : (tj == 20 ? "6, 8 or 10" : "4, 6, 8 or 12"),
+                want);
   }
   int per_sm = 0;
   for (int nv : {12, 10, 8, 6, 4}) {
@@ -542,6 +556,8 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
     if (ok == ST3D_OK) ok = encode_map_t(&p->vhi[f], w16, 2, c->fld[f], c->L, 128, p->tj, 0, 0);
     if (ok == ST3D_OK && hilo)
       ok = encode_map_t(&p->lo[f], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, c->lo[f], c->L, 128, p->tj, 0, 0);
+    else if (ok == ST3D_OK && c->pair)
+      ok = encode_map_t(&p->lo[f], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, c->lo[f], c->L, 128, p->tj, 0, 0);
     else if (ok == ST3D_OK)
       p->lo[f] = p->vhi[f];  // unused by the uncompensated kernels
   }
@@ -621,8 +637,10 @@ FieldRef field_ref(st3d_ctx* c, int f) {
     return r;
   }
   if (c->delta) {  // u = dec(U), v = dec(U) - dec(D)
+    r.storage = word_storage(c->opts.storage);
     r.p = c->fld[c->ub];
     r.E = Eu_buf(c, c->ub);
+    if (c->pair) r.lo16 = (const uint16_t*)c->lo[c->ub];
     if (f == ST3D_FIELD_V) {
       r.p2 = c->fld[3];
       r.E2 = Ed_lvl(c, c->lvl);
@@ -651,7 +669,7 @@ float* stage_slot(st3d_ctx* c, int slot) {
 // Encode a (or a - b) from the staging slots into 16-bit words with per-plane
 // maxima M and scales E; the halo of a (and b) must be zero.
 int encode_staged16(st3d_ctx* c, const float* a, const float* b, void* words, uint32_t* M, int* E,
-                    const char* what) {
+                    const char* what, void* lo16 = nullptr) {
   const st3d_grid_desc& g = c->grid;
   const RefGeom R = ref_geom(g);
   const int hx = g.xh < 4 ? (int)g.xh : 4, hy = g.yh < 4 ? (int)g.yh : 4, hz = (int)g.zh;
@@ -659,8 +677,8 @@ int encode_staged16(st3d_ctx* c, const float* a, const float* b, void* words, ui
   ST3D_CUDA(cudaMemsetAsync(c->halo_max, 0, sizeof(uint32_t), c->stream));
   cudaError_t e = launch_plane_max_ref(R, a, M, c->halo_max, hx, hy, hz, c->stream, b);
   if (e != cudaSuccess) return cuda_fail(e, "plane maximum kernel");
-  e = launch_ref_to_dev16(c->opts.storage, c->L, R, a, (uint16_t*)words, nullptr, M, E, hx, hy, hz,
-                          c->stream, b);
+  e = launch_ref_to_dev16(word_storage(c->opts.storage), c->L, R, a, (uint16_t*)words, nullptr, M, E,
+                          hx, hy, hz, c->stream, b, (uint16_t*)lo16);
   if (e != cudaSuccess) return cuda_fail(e, "16-bit encode kernel");
   uint32_t halo = 0;
   ST3D_CUDA(cudaMemcpyAsync(&halo, c->halo_max, sizeof halo, cudaMemcpyDeviceToHost, c->stream));
@@ -677,10 +695,11 @@ int delta_rebuild_pair(st3d_ctx* c) {
   const RefGeom R = ref_geom(g);
   ST3D_CUDA(cudaMemsetAsync(c->stage, 0, 2 * host_array_bytes(c), c->stream));
   for (int slot = 0; slot < 2; ++slot) {
-    cudaError_t e = launch_delta_to_ref(c->opts.storage, c->L, R, (const uint16_t*)c->fld[c->ub],
-                                        Eu_buf(c, c->ub), (const uint16_t*)c->fld[3],
-                                        Ed_lvl(c, c->lvl), slot == 1, stage_slot(c, slot), (int)g.zh,
-                                        c->stream);
+    cudaError_t e = launch_delta_to_ref(word_storage(c->opts.storage), c->L, R,
+                                        (const uint16_t*)c->fld[c->ub], Eu_buf(c, c->ub),
+                                        (const uint16_t*)c->fld[3], Ed_lvl(c, c->lvl), slot == 1,
+                                        stage_slot(c, slot), (int)g.zh, c->stream,
+                                        (const uint16_t*)c->lo[c->ub]);
     if (e != cudaSuccess) return cuda_fail(e, "16-bit decode kernel");
   }
   c->pair_valid = true;
@@ -693,7 +712,7 @@ int delta_encode_pair(st3d_ctx* c, bool u_changed) {
   c->pair_valid = false;
   if (u_changed &&
       (rc = encode_staged16(c, stage_slot(c, 0), nullptr, c->fld[c->ub], Mu_buf(c, c->ub),
-                            Eu_buf(c, c->ub), "u")) != ST3D_OK)
+                            Eu_buf(c, c->ub), "u", c->pair ? c->lo[c->ub] : nullptr)) != ST3D_OK)
     return rc;
   if ((rc = encode_staged16(c, stage_slot(c, 0), stage_slot(c, 1), c->fld[3], Md_lvl(c, c->lvl),
                             Ed_lvl(c, c->lvl), "u or v")) != ST3D_OK)
@@ -708,9 +727,10 @@ int delta_download(st3d_ctx* c, void* host, bool v) {
   c->pair_valid = false;
   const st3d_grid_desc& g = c->grid;
   const RefGeom R = ref_geom(g);
-  cudaError_t e = launch_delta_to_ref(c->opts.storage, c->L, R, (const uint16_t*)c->fld[c->ub],
-                                      Eu_buf(c, c->ub), (const uint16_t*)c->fld[3], Ed_lvl(c, c->lvl),
-                                      v, stage_slot(c, 0), (int)g.zh, c->stream);
+  cudaError_t e = launch_delta_to_ref(word_storage(c->opts.storage), c->L, R,
+                                      (const uint16_t*)c->fld[c->ub], Eu_buf(c, c->ub),
+                                      (const uint16_t*)c->fld[3], Ed_lvl(c, c->lvl), v, stage_slot(c, 0),
+                                      (int)g.zh, c->stream, (const uint16_t*)c->lo[c->ub]);
   if (e != cudaSuccess) return cuda_fail(e, "16-bit decode kernel");
   const size_t off = ((size_t)g.xh * R.imult + (size_t)g.yh * R.jmult) * 4;
   ST3D_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + off, R.imult * 4,
@@ -904,8 +924,11 @@ int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info
   const int R = radius_of(opts->points);
   const int T = opts->temporal_block > 0 ? opts->temporal_block : 1;
   info->interior_points = (uint64_t)grid->xs * grid->ys * grid->zs;
-  const bool delta = opts->storage == ST3D_F16 || opts->storage == ST3D_BF16;
+  const bool delta = opts->storage == ST3D_F16 || opts->storage == ST3D_BF16 ||
+                     opts->storage == ST3D_F16_HL;
   info->device_bytes = (T > 1 ? 5 : delta ? 4 : 3) * L.elems() * eb;
+  if (opts->storage == ST3D_F16_HL) info->device_bytes += 2 * L.elems() * 2;
+  if (opts->storage == ST3D_F16_HILO) info->device_bytes += 2 * L.elems();
   info->nk = L.nk; info->nj = L.nj; info->ni = L.ni;
   info->pk = L.pk; info->pj = L.pj; info->pi = L.pi;
   info->radius = R;
@@ -970,7 +993,8 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
   const size_t fbytes = c->L.elems() * c->eb;
   // buffers: u/v pair and s; the delta form adds d (3), a context that
   // blocks in time a second u/v pair (3, 4)
-  c->delta = opts->storage == ST3D_F16 || opts->storage == ST3D_BF16;
+  c->delta = opts->storage == ST3D_F16 || opts->storage == ST3D_BF16 || opts->storage == ST3D_F16_HL;
+  c->pair = opts->storage == ST3D_F16_HL;
   const int nbuf = c->opts.temporal_block > 1 ? 5 : c->delta ? 4 : 3;
   for (int f = 0; f < nbuf; ++f) {
     cudaError_t e = cudaMalloc(&c->fld[f], fbytes);
@@ -1017,12 +1041,14 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
   if (c->f16) {
     const size_t xs = grid->xs;
     bool okm = true;
-    if (c->opts.storage == ST3D_F16_HILO)
+    // low parts per u/v buffer: one byte (F16_HILO) or one FP16 word (F16_HL)
+    const size_t lob = c->opts.storage == ST3D_F16_HILO ? c->L.elems() : c->pair ? 2 * c->L.elems() : 0;
+    if (lob)
       for (int f = 0; f < 2; ++f) {
-        okm = okm && cudaMalloc(&c->lo[f], c->L.elems()) == cudaSuccess;
+        okm = okm && cudaMalloc(&c->lo[f], lob) == cudaSuccess;
         if (okm) {
-          c->bytes += c->L.elems();
-          cudaMemsetAsync(c->lo[f], 0, c->L.elems(), c->stream);
+          c->bytes += lob;
+          cudaMemsetAsync(c->lo[f], 0, lob, c->stream);
         }
       }
     okm = okm && cudaMalloc(&c->E, 5 * xs * sizeof(int)) == cudaSuccess &&
@@ -1318,6 +1344,7 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
       st.k4 = c->k4;
       st.m2s = c->m2s;
       st.ubuf = ub;
+      st.lout = c->pair ? (uint16_t*)c->lo[un] : nullptr;
       e = launch_delta16(c->opts.storage, c->opts.points, *c->tma16, c->G, c->cf32, st, src,
                          c->dev_status, c->stream);
       c->pair_valid = false;

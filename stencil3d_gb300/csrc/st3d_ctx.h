@@ -53,6 +53,7 @@ struct st3d_ctx {
   // pair is valid until a step or another use of the slots.
   bool f16 = false;
   bool delta = false;
+  bool pair = false;  // F16_HL: u is an FP16 hi/lo pair, lo[b] the lo words of buffer b
   bool pair_valid = false;
   uint64_t lvl = 0;
   float m2s = 0.0f;

@@ -160,9 +160,10 @@ struct Delta16Step {
   uint32_t *Mu_out, *Md_out;       // maxima of the new levels
   float k4, m2s;
   int ubuf;                        // buffer holding u^n
+  uint16_t* lout = nullptr;        // F16_HL: lo words of u^{n+1} (those of u^n: plan map lo[ubuf])
 };
 struct Tma16Plan;
-size_t delta16_smem_bytes(int tj, int nv, int R);
+size_t delta16_smem_bytes(int tj, int nv, int R, bool pair = false);
 int delta16_blocks_per_sm(int storage, int points, const Tma16Plan& pl);
 cudaError_t launch_delta16(int storage, int points, const Tma16Plan& pl, const Geom& g,
                            const Coefs<float>& cf, const Delta16Step& st, const Source& src,
@@ -179,14 +180,18 @@ cudaError_t launch_tma16(int storage, int points, const Tma16Plan& pl, const Geo
 cudaError_t launch_plane_max_ref(const RefGeom& R, const float* stage, uint32_t* M,
                                  uint32_t* halo_max, int hx, int hy, int hz, cudaStream_t stream,
                                  const float* stage2 = nullptr);
+// With `lo16` (F16 words only), also the lo words of the FP16 hi/lo pair.
 cudaError_t launch_ref_to_dev16(int storage, const Layout& L, const RefGeom& R, const float* stage,
                                 uint16_t* hi, int8_t* lo, const uint32_t* M, int* E, int hx, int hy,
-                                int hz, cudaStream_t stream, const float* stage2 = nullptr);
+                                int hz, cudaStream_t stream, const float* stage2 = nullptr,
+                                uint16_t* lo16 = nullptr);
 // Delta form -> reference layout: u = dec(U) (minus_d false) or
 // v = dec(U) - dec(D) (minus_d true), interior rows with their k halo.
+// With `ul` (the F16_HL form) u = (U + ul) * 2^Eu.
 cudaError_t launch_delta_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* u,
                                 const int* Eu, const uint16_t* d, const int* Ed, bool minus_d,
-                                float* stage, int hz, cudaStream_t stream);
+                                float* stage, int hz, cudaStream_t stream,
+                                const uint16_t* ul = nullptr);
 cudaError_t launch_dev16_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* hi,
                                 const int8_t* lo, const int* E, float* stage, int hz,
                                 cudaStream_t stream);
@@ -216,6 +221,7 @@ struct FieldRef {
   const int* E;
   const void* p2 = nullptr;  // delta form: the value is dec(p) - dec(p2)
   const int* E2 = nullptr;
+  const uint16_t* lo16 = nullptr;  // F16_HL: dec(p) = (hi + lo16) * 2^E
 };
 cudaError_t launch_check(const Geom& g, const FieldRef& v, double expected, double tol,
                          unsigned long long* counter, cudaStream_t stream);

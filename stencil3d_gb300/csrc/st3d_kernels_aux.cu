@@ -86,6 +86,7 @@ __device__ __forceinline__ double load_field(const FieldRef& f, long long i, lon
       const uint16_t w = static_cast<const uint16_t*>(f.p)[x];
       float v = __half2float(__ushort_as_half(w));
       if (f.lo) v = __fmaf_rn((float)f.lo[x], ulp256_f16(w), v);
+      if (f.lo16) v = v + __half2float(__ushort_as_half(f.lo16[x]));  // exact: <= 22 bits
       v = v * exp2i(f.E[i]);
       if (f.p2) v = v - __half2float(__ushort_as_half(static_cast<const uint16_t*>(f.p2)[x])) * exp2i(f.E2[i]);
       return (double)v;

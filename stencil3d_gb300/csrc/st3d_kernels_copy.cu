@@ -154,11 +154,13 @@ __global__ void k_plane_max_ref(RefGeom R, const float* __restrict__ stage,
 
 // Scatter + encode: staging (reference layout, float) -> words (+ low bytes)
 // in the library layout, the plane's scale from its maximum.
+// With lo16 (FP16 words), the lo word of the hi/lo pair: fp16(xs - hi).
 template <int KIND, bool HILO>
 __global__ void k_ref_to_dev16(Layout L, RefGeom R, const float* __restrict__ stage,
                                const float* __restrict__ stage2, uint16_t* __restrict__ hi,
                                int8_t* __restrict__ lo, const uint32_t* __restrict__ M,
-                               int* __restrict__ E, int hx, int hy, int hz) {
+                               int* __restrict__ E, int hx, int hy, int hz,
+                               uint16_t* __restrict__ lo16) {
   const int kk = blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= R.zs + 2 * hz) return;
   const int j = (int)blockIdx.y - hy;
@@ -172,6 +174,7 @@ __global__ void k_ref_to_dev16(Layout L, RefGeom R, const float* __restrict__ st
   const long long d = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
   const uint16_t w = float_to_word<KIND>(xs);
   hi[d] = w;
+  if (lo16) lo16[d] = float_to_word<KIND>(xs - word_to_float<KIND>(w));
   if (HILO) {
     const float r = xs - word_to_float<KIND>(w);
     int eb = (w >> 10) & 0x1f;
@@ -205,14 +208,16 @@ template <int KIND>
 __global__ void k_delta_to_ref(Layout L, RefGeom R, const uint16_t* __restrict__ u,
                                const int* __restrict__ Eu, const uint16_t* __restrict__ d,
                                const int* __restrict__ Ed, bool minus_d, float* __restrict__ stage,
-                               int hz) {
+                               int hz, const uint16_t* __restrict__ ul) {
   const int kk = blockIdx.x * blockDim.x + threadIdx.x;
   if (kk >= R.zs + 2 * hz) return;
   const int j = (int)blockIdx.y;
   const int i = (int)blockIdx.z;
   const int k = kk - hz;
   const long long s = ((long long)(i + (int)L.pi) * L.nj + (j + (int)L.pj)) * L.nk + (k + (int)L.pk);
-  float x = word_to_float<KIND>(u[s]) * exp2i(Eu[i]);
+  float x = word_to_float<KIND>(u[s]);
+  if (ul) x = x + word_to_float<KIND>(ul[s]);  // exact: the pair holds <= 22 bits
+  x = x * exp2i(Eu[i]);
   if (minus_d) x = x - word_to_float<KIND>(d[s]) * exp2i(Ed[i]);
   stage[R.ijk_ofs + (long long)i * R.imult + (long long)j * R.jmult + k] = x;
 }
@@ -231,16 +236,17 @@ cudaError_t launch_plane_max_ref(const RefGeom& R, const float* stage, uint32_t*
 
 cudaError_t launch_ref_to_dev16(int storage, const Layout& L, const RefGeom& R, const float* stage,
                                 uint16_t* hi, int8_t* lo, const uint32_t* M, int* E, int hx, int hy,
-                                int hz, cudaStream_t stream, const float* stage2) {
+                                int hz, cudaStream_t stream, const float* stage2, uint16_t* lo16) {
   dim3 block(256);
   dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys + 2 * hy, R.xs + 2 * hx);
   if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
+  if (lo16 && storage != ST3D_F16) return cudaErrorInvalidValue;
   if (storage == ST3D_F16)
-    k_ref_to_dev16<0, false><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz);
+    k_ref_to_dev16<0, false><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz, lo16);
   else if (storage == ST3D_BF16)
-    k_ref_to_dev16<1, false><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz);
+    k_ref_to_dev16<1, false><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz, lo16);
   else if (storage == ST3D_F16_HILO)
-    k_ref_to_dev16<0, true><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz);
+    k_ref_to_dev16<0, true><<<grid, block, 0, stream>>>(L, R, stage, stage2, hi, lo, M, E, hx, hy, hz, lo16);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
@@ -248,14 +254,15 @@ cudaError_t launch_ref_to_dev16(int storage, const Layout& L, const RefGeom& R, 
 
 cudaError_t launch_delta_to_ref(int storage, const Layout& L, const RefGeom& R, const uint16_t* u,
                                 const int* Eu, const uint16_t* d, const int* Ed, bool minus_d,
-                                float* stage, int hz, cudaStream_t stream) {
+                                float* stage, int hz, cudaStream_t stream, const uint16_t* ul) {
   dim3 block(256);
   dim3 grid((R.zs + 2 * hz + 255) / 256, R.ys, R.xs);
   if (grid.y > 65535 || grid.z > 65535) return cudaErrorInvalidConfiguration;
+  if (ul && storage != ST3D_F16) return cudaErrorInvalidValue;
   if (storage == ST3D_F16)
-    k_delta_to_ref<0><<<grid, block, 0, stream>>>(L, R, u, Eu, d, Ed, minus_d, stage, hz);
+    k_delta_to_ref<0><<<grid, block, 0, stream>>>(L, R, u, Eu, d, Ed, minus_d, stage, hz, ul);
   else if (storage == ST3D_BF16)
-    k_delta_to_ref<1><<<grid, block, 0, stream>>>(L, R, u, Eu, d, Ed, minus_d, stage, hz);
+    k_delta_to_ref<1><<<grid, block, 0, stream>>>(L, R, u, Eu, d, Ed, minus_d, stage, hz, ul);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

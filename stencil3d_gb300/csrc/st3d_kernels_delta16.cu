@@ -75,6 +75,7 @@ struct Delta16Args {
   Source src;
   uint64_t timeout_ns;
   uint32_t* status;
+  uint16_t* lout;  // PAIR: lo words of u^{n+1}
 };
 
 __device__ __forceinline__ float amax4(const P4& x, bool c0, bool c1, bool c2, bool c3, float m) {
@@ -86,11 +87,14 @@ __device__ __forceinline__ float amax4(const P4& x, bool c0, bool c1, bool c2, b
 }
 
 // TJ = 16 or 20 rows: one CTA of 17 or 21 warps per SM; TJ = 8: two CTAs of
-// 9 warps.
-template <int KIND, int P, int TJ, int NV>
+// 9 warps.  PAIR (the F16_HL form, FP16 words): u^n also has lo words (lmap,
+// a third tile per stage for the centre plane); the centre u is hi + lo, the
+// neighbours the hi words, and u^{n+1} is written as a pair.
+template <int KIND, int P, int TJ, int NV, bool PAIR>
 __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
     k_delta16(const __grid_constant__ CUtensorMap umap, const __grid_constant__ CUtensorMap dmap,
-              const __grid_constant__ CUtensorMap smap, const Delta16Args a) {
+              const __grid_constant__ CUtensorMap smap, const __grid_constant__ CUtensorMap lmap,
+              const Delta16Args a) {
   constexpr int R = RadD<P>::value;
   constexpr int QN = 2 * R + 1;
   constexpr int NU = NV + R;
@@ -103,7 +107,8 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
   unsigned char* ur = smem;
   unsigned char* dr = ur + NU * USLOT;
   unsigned char* sr = dr + NV * VSLOT;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sr + NV * VSLOT);
+  unsigned char* lr = sr + NV * VSLOT;  // PAIR: lo words of the centre plane of u
+  uint64_t* full = reinterpret_cast<uint64_t*>(lr + (PAIR ? NV * VSLOT : 0));
   uint64_t* empty = full + NV;
   StageScales* info = reinterpret_cast<StageScales*>(empty + NV);
   uint32_t* smax_u = reinterpret_cast<uint32_t*>(info + NV);
@@ -134,6 +139,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
       tma_prefetch_desc(&umap);
       tma_prefetch_desc(&dmap);
       tma_prefetch_desc(&smap);
+      if (PAIR) tma_prefetch_desc(&lmap);
     }
     uint32_t h = 0;
     bool ok = true;
@@ -200,13 +206,15 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
             const bool has_ds = n >= 2 * R;
             splane[stage] = has_ds ? ia + n - 2 * R : -1;
             info[stage] = si;
-            mbar_arrive_expect_tx(&full[stage], UBYTES + (has_ds ? 2u * VSLOT : 0u));
+            mbar_arrive_expect_tx(&full[stage], UBYTES + (has_ds ? (PAIR ? 3u : 2u) * VSLOT : 0u));
             tma_load_3d(ur + (h % NU) * USLOT, &umap, &full[stage], g.pk + k0 - kKH, g.pj + j0 - R,
                         g.pi + p);
             if (has_ds) {
               const int i = ia + n - 2 * R;
               tma_load_3d(dr + stage * VSLOT, &dmap, &full[stage], g.pk + k0, g.pj + j0, g.pi + i);
               tma_load_3d(sr + stage * VSLOT, &smap, &full[stage], g.pk + k0, g.pj + j0, g.pi + i);
+              if (PAIR)
+                tma_load_3d(lr + stage * VSLOT, &lmap, &full[stage], g.pk + k0, g.pj + j0, g.pi + i);
             }
           }
           __syncwarp();
@@ -292,7 +300,15 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
           const float2 r01 = w2_to_f2<KIND>(wr.x), r23 = w2_to_f2<KIND>(wr.y);
           const float w[12] = {l01.x, l01.y, l23.x, l23.y, c01.x, c01.y, c23.x, c23.y,
                                r01.x, r01.y, r23.x, r23.y};
-          const P4 u0 = {__fmul2_rn(c01, splat(si.uc)), __fmul2_rn(c23, splat(si.uc))};
+          P4 u0;
+          if (PAIR) {
+            // the whole pair: hi + lo is exact in float (at most 22 bits)
+            const uint2 lw = *reinterpret_cast<const uint2*>(lr + stage * VSLOT + (r * kTK + 4 * lane) * 2);
+            u0 = {__fmul2_rn(__fadd2_rn(c01, w2_to_f2<KIND>(lw.x)), splat(si.uc)),
+                  __fmul2_rn(__fadd2_rn(c23, w2_to_f2<KIND>(lw.y)), splat(si.uc))};
+          } else {
+            u0 = {__fmul2_rn(c01, splat(si.uc)), __fmul2_rn(c23, splat(si.uc))};
+          }
           P4 acc;
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
@@ -341,7 +357,18 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
           const uint2 dwo = encode4<KIND>(dn, si.inv_do);
           const P4 dq = decode4<KIND>(dwo, si.dq);
           const P4 un = add4(u0, dq);
-          const uint2 uwo = encode4<KIND>(un, si.inv_uo);
+          uint2 uwo, ulo = make_uint2(0u, 0u);
+          if (PAIR) {
+            // hi = fp16(t), lo = fp16(t - hi): t - hi is exact in float
+            const float2 t01 = __fmul2_rn(un.a, splat(si.inv_uo));
+            const float2 t23 = __fmul2_rn(un.b, splat(si.inv_uo));
+            uwo = make_uint2(f2_to_w2<KIND>(t01), f2_to_w2<KIND>(t23));
+            const float2 h01 = w2_to_f2<KIND>(uwo.x), h23 = w2_to_f2<KIND>(uwo.y);
+            ulo = make_uint2(f2_to_w2<KIND>(__fadd2_rn(t01, make_float2(-h01.x, -h01.y))),
+                             f2_to_w2<KIND>(__fadd2_rn(t23, make_float2(-h23.x, -h23.y))));
+          } else {
+            uwo = encode4<KIND>(un, si.inv_uo);
+          }
           mu = amax4(un, k0ok, k1ok, k2ok, k3ok, mu);
           md = amax4(dn, k0ok, k1ok, k2ok, k3ok, md);
           if (row_ok) {
@@ -349,16 +376,20 @@ __global__ void __launch_bounds__((TJ + 1) * 32, TJ == 8 ? 2 : 1)
             if (k3ok) {
               *reinterpret_cast<uint2*>(a.uout + x0) = uwo;
               *reinterpret_cast<uint2*>(a.d + x0) = dwo;
+              if (PAIR) *reinterpret_cast<uint2*>(a.lout + x0) = ulo;
             } else {
               const uint16_t uo[4] = {(uint16_t)(uwo.x & 0xffff), (uint16_t)(uwo.x >> 16),
                                       (uint16_t)(uwo.y & 0xffff), (uint16_t)(uwo.y >> 16)};
               const uint16_t do_[4] = {(uint16_t)(dwo.x & 0xffff), (uint16_t)(dwo.x >> 16),
                                        (uint16_t)(dwo.y & 0xffff), (uint16_t)(dwo.y >> 16)};
+              const uint16_t lo_[4] = {(uint16_t)(ulo.x & 0xffff), (uint16_t)(ulo.x >> 16),
+                                       (uint16_t)(ulo.y & 0xffff), (uint16_t)(ulo.y >> 16)};
 #pragma unroll
               for (int c = 0; c < 4; ++c)
                 if (k + c < g.zs) {
                   a.uout[x0 + c] = uo[c];
                   a.d[x0 + c] = do_[c];
+                  if (PAIR) a.lout[x0 + c] = lo_[c];
                 }
             }
           }
@@ -401,73 +432,89 @@ __global__ void k_scales_delta(int xs, int R, const uint32_t* __restrict__ Mu, c
   Md_out[i] = 0u;
 }
 
-template <int KIND, int P, int TJ, int NV>
+template <int KIND, int P, int TJ, int NV, bool PAIR>
 cudaError_t launch_nv(const Tma16Plan& pl, const Delta16Args& args, const CUtensorMap* maps,
                       cudaStream_t stream, int* occupancy_out) {
-  auto kern = k_delta16<KIND, P, TJ, NV>;
+  auto kern = k_delta16<KIND, P, TJ, NV, PAIR>;
   const int threads = (TJ + 1) * 32;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
   if (e != cudaSuccess) return e;
   if (occupancy_out) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occupancy_out, kern, threads, pl.smem);
-  kern<<<pl.grid, threads, pl.smem, stream>>>(maps[0], maps[1], maps[2], args);
+  kern<<<pl.grid, threads, pl.smem, stream>>>(maps[0], maps[1], maps[2], maps[3], args);
   return cudaGetLastError();
 }
 
 // Pipeline depths per tile height: 8 and 16 rows take 4/6/8/12 stages; 20
 // rows (21 warps, 80 registers) take 6/8/10, the depths that fit 227 KB.
-template <int KIND, int P, int TJ>
+// The pair form carries a third tile per stage: 4/6/8, and 6/8 on 20 rows.
+template <int KIND, int P, int TJ, bool PAIR>
 cudaError_t launch_tj(const Tma16Plan& pl, const Delta16Args& args, const CUtensorMap* maps,
                       cudaStream_t stream, int* occ) {
-  if (TJ == 20) {
+  if constexpr (PAIR && TJ == 20) {
     switch (pl.nv) {
-      case 6: return launch_nv<KIND, P, TJ, 6>(pl, args, maps, stream, occ);
-      case 8: return launch_nv<KIND, P, TJ, 8>(pl, args, maps, stream, occ);
-      case 10: return launch_nv<KIND, P, TJ, 10>(pl, args, maps, stream, occ);
+      case 6: return launch_nv<KIND, P, TJ, 6, PAIR>(pl, args, maps, stream, occ);
+      case 8: return launch_nv<KIND, P, TJ, 8, PAIR>(pl, args, maps, stream, occ);
+      default: return cudaErrorInvalidConfiguration;
+    }
+  } else if constexpr (PAIR) {
+    switch (pl.nv) {
+      case 4: return launch_nv<KIND, P, TJ, 4, PAIR>(pl, args, maps, stream, occ);
+      case 6: return launch_nv<KIND, P, TJ, 6, PAIR>(pl, args, maps, stream, occ);
+      case 8: return launch_nv<KIND, P, TJ, 8, PAIR>(pl, args, maps, stream, occ);
+      default: return cudaErrorInvalidConfiguration;
+    }
+  } else if constexpr (TJ == 20) {
+    switch (pl.nv) {
+      case 6: return launch_nv<KIND, P, TJ, 6, PAIR>(pl, args, maps, stream, occ);
+      case 8: return launch_nv<KIND, P, TJ, 8, PAIR>(pl, args, maps, stream, occ);
+      case 10: return launch_nv<KIND, P, TJ, 10, PAIR>(pl, args, maps, stream, occ);
+      default: return cudaErrorInvalidConfiguration;
+    }
+  } else {
+    switch (pl.nv) {
+      case 4: return launch_nv<KIND, P, TJ, 4, PAIR>(pl, args, maps, stream, occ);
+      case 6: return launch_nv<KIND, P, TJ, 6, PAIR>(pl, args, maps, stream, occ);
+      case 8: return launch_nv<KIND, P, TJ, 8, PAIR>(pl, args, maps, stream, occ);
+      case 12: return launch_nv<KIND, P, TJ, 12, PAIR>(pl, args, maps, stream, occ);
       default: return cudaErrorInvalidConfiguration;
     }
   }
-  switch (pl.nv) {
-    case 4: return launch_nv<KIND, P, TJ, 4>(pl, args, maps, stream, occ);
-    case 6: return launch_nv<KIND, P, TJ, 6>(pl, args, maps, stream, occ);
-    case 8: return launch_nv<KIND, P, TJ, 8>(pl, args, maps, stream, occ);
-    case 12: return launch_nv<KIND, P, TJ, 12>(pl, args, maps, stream, occ);
-    default: return cudaErrorInvalidConfiguration;
-  }
 }
 
-template <int KIND, int P>
+template <int KIND, int P, bool PAIR>
 cudaError_t launch_p(const Tma16Plan& pl, const Delta16Args& args, const CUtensorMap* maps,
                      cudaStream_t stream, int* occ) {
-  if (pl.tj == 16) return launch_tj<KIND, P, 16>(pl, args, maps, stream, occ);
-  if (pl.tj == 20) return launch_tj<KIND, P, 20>(pl, args, maps, stream, occ);
-  if (pl.tj == 8) return launch_tj<KIND, P, 8>(pl, args, maps, stream, occ);
+  if (pl.tj == 16) return launch_tj<KIND, P, 16, PAIR>(pl, args, maps, stream, occ);
+  if (pl.tj == 20) return launch_tj<KIND, P, 20, PAIR>(pl, args, maps, stream, occ);
+  if (pl.tj == 8) return launch_tj<KIND, P, 8, PAIR>(pl, args, maps, stream, occ);
   return cudaErrorInvalidConfiguration;
 }
 
-template <int KIND>
+template <int KIND, bool PAIR>
 cudaError_t launch_k(int points, const Tma16Plan& pl, const Delta16Args& args, const CUtensorMap* maps,
                      cudaStream_t stream, int* occ) {
   switch (points) {
-    case 7: return launch_p<KIND, 7>(pl, args, maps, stream, occ);
-    case 13: return launch_p<KIND, 13>(pl, args, maps, stream, occ);
-    case 25: return launch_p<KIND, 25>(pl, args, maps, stream, occ);
+    case 7: return launch_p<KIND, 7, PAIR>(pl, args, maps, stream, occ);
+    case 13: return launch_p<KIND, 13, PAIR>(pl, args, maps, stream, occ);
+    case 25: return launch_p<KIND, 25, PAIR>(pl, args, maps, stream, occ);
     default: return cudaErrorInvalidValue;
   }
 }
 
 cudaError_t dispatch(int storage, int points, const Tma16Plan& pl, const Delta16Args& args,
                      const CUtensorMap* maps, cudaStream_t stream, int* occ) {
-  if (storage == ST3D_F16) return launch_k<0>(points, pl, args, maps, stream, occ);
-  if (storage == ST3D_BF16) return launch_k<1>(points, pl, args, maps, stream, occ);
+  if (storage == ST3D_F16) return launch_k<0, false>(points, pl, args, maps, stream, occ);
+  if (storage == ST3D_BF16) return launch_k<1, false>(points, pl, args, maps, stream, occ);
+  if (storage == ST3D_F16_HL) return launch_k<0, true>(points, pl, args, maps, stream, occ);
   return cudaErrorInvalidValue;
 }
 
 }  // namespace
 
-size_t delta16_smem_bytes(int tj, int nv, int R) {
+size_t delta16_smem_bytes(int tj, int nv, int R, bool pair) {
   const size_t uslot = ((size_t)kUKW * (tj + 2 * R) * 2 + 127) / 128 * 128;
   const size_t vslot = (size_t)kTK * tj * 2;
-  return (size_t)(nv + R) * uslot + 2 * (size_t)nv * vslot +
+  return (size_t)(nv + R) * uslot + (pair ? 3 : 2) * (size_t)nv * vslot +
          2 * (size_t)nv * 8 + (size_t)nv * sizeof(StageScales) + 3 * (size_t)nv * 4 + 128;
 }
 
@@ -504,7 +551,9 @@ cudaError_t launch_delta16(int storage, int points, const Tma16Plan& pl, const G
   a.src = src;
   a.timeout_ns = pl.timeout_ns;
   a.status = dev_status;
-  const CUtensorMap maps[3] = {pl.uhi[st.ubuf], pl.dmap, pl.vhi[2]};
+  a.lout = st.lout;
+  if (pl.pair != (st.lout != nullptr)) return cudaErrorInvalidValue;
+  const CUtensorMap maps[4] = {pl.uhi[st.ubuf], pl.dmap, pl.vhi[2], pl.lo[st.ubuf]};
   k_scales_delta<<<(g.xs + 255) / 256, 256, 0, stream>>>(g.xs, pl.radius, st.Mu, st.Md, st.Ms,
                                                          st.Eu_out, st.Ed_out, st.Mu_out, st.Md_out,
                                                          st.k4, cf.c2, src.i, fabsf(src.amp));

@@ -40,6 +40,7 @@ struct Tma16Plan {
   size_t smem = 0;
   uint64_t timeout_ns = 4000000000ull;
   bool delta = false;     // FP16 / BF16 delta form (st3d_kernels_delta16.cu)
+  bool pair = false;      // F16_HL: u as an FP16 hi/lo pair; lo[] are its lo words
   CUtensorMap uhi[2];
   CUtensorMap vhi[3];
   CUtensorMap lo[2];

@@ -11,7 +11,7 @@
 // --wave (the leapfrog form, README.md:11-20, with --vel/--dt/--dx),
 // --kernel simple|tma|auto, --variant ref|vec8|vec16 (the reference's
 // compile-time kernel variant whose results to reproduce), --storage
-// f32|f16|bf16|f16_hilo (device storage of the wave form) and
+// f32|f16|bf16|f16_hilo|f16_hl (device storage of the wave form) and
 // --temporal-block 1|2|4 (FP32 wave steps fused per pass).
 #include <cstdio>
 #include <cstdlib>
@@ -128,8 +128,9 @@ int main(int argc, char** argv) {
   else if (strcmp(storage, "f16") == 0) gopt.storage = ST3D_F16;
   else if (strcmp(storage, "bf16") == 0) gopt.storage = ST3D_BF16;
   else if (strcmp(storage, "f16_hilo") == 0) gopt.storage = ST3D_F16_HILO;
+  else if (strcmp(storage, "f16_hl") == 0) gopt.storage = ST3D_F16_HL;
   else {
-    fprintf(stderr, "--storage must be f32, f16, bf16 or f16_hilo\n");
+    fprintf(stderr, "--storage must be f32, f16, bf16, f16_hilo or f16_hl\n");
     return 2;
   }
   if (gopt.storage != ST3D_F32 && !wave) {

@@ -15,7 +15,7 @@ GRID = S.Grid(256, 256, 256, 4, 4, 4)
 @pytest.mark.parametrize("points,mode,storage", [
     (25, "wave", "f32"), (13, "wave", "f32"), (7, "wave", "f32"), (7, "ref", "f32"),
     (25, "ref", "f64"), (2, "ref", "f32"), (25, "wave", "f16"), (13, "wave", "bf16"),
-    (7, "wave", "f16_hilo")])
+    (7, "wave", "f16_hilo"), (25, "wave", "f16_hl"), (7, "wave", "f16_hl")])
 def test_candidates_are_accepted_by_the_planner(points, mode, storage):
     cands = autotune.candidates(points, mode, storage, zero_halo=True)
     assert cands

@@ -1,6 +1,7 @@
 """GPU parity of the precision forms, all arithmetic in FP32:
   - FP16 / BF16: u and the time difference d = u^n - u^{n-1} in 16-bit
     words with a power-of-two scale per i-plane (the delta form);
+  - FP16 hi/lo pair: the delta form with u held as two FP16 words;
   - FP16 + a compensating byte: u and v in FP16 words plus a low byte.
 
 The library's 16-bit kernels and the oracle's restatement of the same
@@ -30,7 +31,7 @@ def _inputs(grid, seed, blobs):
     return np.ascontiguousarray(v), s, u
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_hilo"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_hilo", "f16_hl"])
 @pytest.mark.parametrize("points", [7, 13, 25])
 @pytest.mark.parametrize("grid,blobs", [((24, 40, 150, 4, 4, 4), True),
                                         ((9, 17, 64, 4, 4, 16), False)])
@@ -50,8 +51,10 @@ def test_f16_forms_match_oracle(storage, points, grid, blobs):
 
 
 @pytest.mark.parametrize("points", [7, 25])
-@pytest.mark.parametrize("tile_j,stages", [(16, 12), (16, 4), (20, 10), (20, 6), (8, 8)])
-def test_delta_form_tiles_match_oracle(points, tile_j, stages):
+@pytest.mark.parametrize("storage,tile_j,stages", [
+    ("f16", 16, 12), ("f16", 16, 4), ("f16", 20, 10), ("f16", 20, 6), ("f16", 8, 8),
+    ("f16_hl", 16, 8), ("f16_hl", 20, 8), ("f16_hl", 20, 6), ("f16_hl", 8, 4)])
+def test_delta_form_tiles_match_oracle(points, storage, tile_j, stages):
     """Every tile height and pipeline depth of the delta kernel gives the
     oracle's bits; ys = 43 leaves a partial tile for 8, 16 and 20 rows."""
     grid = (30, 43, 140, 4, 4, 4)
@@ -59,12 +62,12 @@ def test_delta_form_tiles_match_oracle(points, tile_j, stages):
     steps = 7
     src = (15, 21, 70)
     v, s, u = _inputs(grid, 40 + points, True)
-    with S.Stencil(S.Grid(*grid), points, "wave", "f16", dt=dt, src=src, tile_j=tile_j,
+    with S.Stencil(S.Grid(*grid), points, "wave", storage, dt=dt, src=src, tile_j=tile_j,
                    stages=stages) as st:
         assert st.info().tile_j == tile_j
         uu, vv = u.copy(), v.copy()
         st.iterate_host(vv, s, uu, steps)
-    ou, ov = _oracle_run("f16", u, v, s, grid, points, steps, dt, src)
+    ou, ov = _oracle_run(storage, u, v, s, grid, points, steps, dt, src)
     np.testing.assert_array_equal(O.interior(uu, grid), O.interior(ou, grid))
     np.testing.assert_array_equal(O.interior(vv, grid), O.interior(ov, grid))
 
@@ -76,7 +79,7 @@ def _oracle_run(storage, u, v, s, grid, points, steps, dt, src=None, t0=0):
     amps = O.ricker_amps(t0, steps, dt)
     fs = O.Field16(s, grid, kind, hilo and False)
     if not hilo:
-        fu, fd = O.delta_fields(u, v, grid, kind)
+        fu, fd = O.delta_fields(u, v, grid, kind, pair=storage == "f16_hl")
         O.iterate_delta16(fu, fd, fs, grid, points, steps, np.float32(c1), np.float32(c2), src=src,
                           amps=amps)
         return O.delta_decode(fu, fd)
@@ -86,7 +89,8 @@ def _oracle_run(storage, u, v, s, grid, points, steps, dt, src=None, t0=0):
     return fu.decode(), fv.decode()
 
 
-@pytest.mark.parametrize("storage,bound", [("f16_hilo", 3e-4), ("f16", 3e-3), ("bf16", 2e-2)])
+@pytest.mark.parametrize("storage,bound", [("f16_hilo", 3e-4), ("f16_hl", 6e-4), ("f16", 3e-3),
+                                           ("bf16", 2e-2)])
 def test_f16_forms_track_fp64(storage, bound):
     """Accuracy of each form against FP64 after 60 steps of a smooth field."""
     grid = (32, 36, 140, 4, 4, 4)
@@ -129,7 +133,7 @@ def test_f16_norms_and_fill():
         assert np.all(u[halo_mask(grid)] == 0.0)
 
 
-@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f16_hl"])
 def test_delta_form_partial_uploads_and_fills(storage):
     """Setting u or v alone rebuilds the pair from the device state first;
     fills go through the same path; norms of v decode u - d."""
@@ -146,11 +150,14 @@ def test_delta_form_partial_uploads_and_fills(storage):
         st.upload(v=v)
         ua, va = g.empty(), g.empty()
         st.download(va, ua)
-        np.testing.assert_array_equal(g.interior(ua), g.interior(u3))
-        # v comes back as dec(U) - dec(D) with D = enc(u3 - v)
+        # u re-encoded from u3 (its own plane scales), v = dec(U) - dec(D)
+        # with D = enc(u3 - v)
         kind, _ = O.storage_kind(storage)
-        _, fd = O.delta_fields(u3, v, grid, kind)
-        np.testing.assert_array_equal(g.interior(va), O.interior(u3 - fd.decode(), grid))
+        fu, fd = O.delta_fields(u3, v, grid, kind, pair=storage == "f16_hl")
+        eu, ev = O.delta_decode(fu, fd)
+        np.testing.assert_array_equal(g.interior(ua), O.interior(eu, grid))
+        np.testing.assert_array_equal(g.interior(va), O.interior(ev, grid))
+        assert np.max(np.abs(g.interior(ua) - g.interior(u3))) <= 2.0 ** -20 * np.max(np.abs(u3))
         # device norms of v decode the same values
         e2, _, em, _ = st.norms(S.FIELD_V)
         vi = g.interior(va).astype(np.float64)

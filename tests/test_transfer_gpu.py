@@ -2,8 +2,8 @@
 
   - a transfer between two FP32 contexts carries the whole time state: both
     continue bit for bit alike, source clock included;
-  - a transfer from FP16 delta storage into the compensated storage equals
-    the host round trip (download into host arrays, upload, set_step);
+  - a transfer from FP16 delta storage into either compensated storage
+    equals the host round trip (download into host arrays, upload, set_step);
   - upload and download take device arrays of the reference layout and move
     the same values as host arrays;
   - mismatched contexts are refused before anything moves.
@@ -58,7 +58,8 @@ def test_transfer_fp32_continues_alike(points):
     np.testing.assert_array_equal(va, vb)
 
 
-def test_transfer_equals_host_round_trip():
+@pytest.mark.parametrize("fallback", ["f16_hilo", "f16_hl"])
+def test_transfer_equals_host_round_trip(fallback):
     g = S.Grid(*GRID)
     v, s, u = _inputs(8)
     with S.Stencil(g, 25, "wave", "f16", dt=5e-4, src=SRC) as a:
@@ -67,8 +68,8 @@ def test_transfer_equals_host_round_trip():
         hu, hv = g.empty(), g.empty()
         a.download(hv, hu)
         a.synchronize()
-        with S.Stencil(g, 25, "wave", "f16_hilo", dt=5e-4, src=SRC) as dev, \
-                S.Stencil(g, 25, "wave", "f16_hilo", dt=5e-4, src=SRC) as host:
+        with S.Stencil(g, 25, "wave", fallback, dt=5e-4, src=SRC) as dev, \
+                S.Stencil(g, 25, "wave", fallback, dt=5e-4, src=SRC) as host:
             dev.upload(None, s, None)
             dev.transfer_from(a)
             host.upload(hv, s, hu)
