@@ -10,7 +10,8 @@
 // TMA (the grid's own tensor maps, kept in global memory) and tells the
 // consumer warps which item each pipeline stage belongs to; the consumers run
 // the stencil of the item's order (the same code and arithmetic as the
-// single-grid TMA kernel).  Steps are ordered by kernel boundaries; the whole
+// single-grid TMA kernel, on packed FP32 pairs: 243 -> 278 Gpts/s on the
+// 64-grid batch against scalar FP32).  Steps are ordered by kernel boundaries; the whole
 // time loop (a queue reset and a launch per step) can be captured in a CUDA
 // graph and replayed.  The baseline schedule launches the single-grid kernel
 // once per grid per step.
@@ -22,6 +23,7 @@
 
 #include "st3d_ctx.h"
 #include "st3d_internal.h"
+#include "st3d_p4.cuh"
 #include "st3d_tma.cuh"
 
 namespace st3d {
@@ -116,47 +118,49 @@ __device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid
         const float4 l4 = *reinterpret_cast<const float4*>(uc + 4 * lane);
         const float4 r4 = *reinterpret_cast<const float4*>(uc + 2 * kTmaKHalo + 4 * lane);
         const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w, r4.x, r4.y, r4.z, r4.w};
-        float acc[4];
+        const P4 cu = {make_float2(c4.x, c4.y), make_float2(c4.z, c4.w)};
+        const P4 u2 = add4(cu, cu);
+        const P4 nu2 = {make_float2(-u2.a.x, -u2.a.y), make_float2(-u2.b.x, -u2.b.y)};
+        P4 acc;
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
           const int ax = pair_axis(P, p);
           const int rr = pair_r(P, p);
-          float av[4], bv[4];
-          if (ax == 2) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              av[c] = w[4 + c - rr];
-              bv[c] = w[4 + c + rr];
-            }
+          P4 sum;
+          if (ax == 2 && (rr & 1)) {
+            sum = {make_float2(w[4 - rr] + w[4 + rr], w[5 - rr] + w[5 + rr]),
+                   make_float2(w[6 - rr] + w[6 + rr], w[7 - rr] + w[7 + rr])};
+          } else if (ax == 2) {
+            sum = add4({make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])},
+                       {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])});
           } else if (ax == 1) {
             const float4 A = *reinterpret_cast<const float4*>(uc - rr * UKW + kTmaKHalo + 4 * lane);
             const float4 B = *reinterpret_cast<const float4*>(uc + rr * UKW + kTmaKHalo + 4 * lane);
-            av[0] = A.x; av[1] = A.y; av[2] = A.z; av[3] = A.w;
-            bv[0] = B.x; bv[1] = B.y; bv[2] = B.z; bv[3] = B.w;
+            sum = add4({make_float2(A.x, A.y), make_float2(A.z, A.w)},
+                       {make_float2(B.x, B.y), make_float2(B.z, B.w)});
           } else {
             const float4 A = q[(ph + 2 * QN - R - rr) % QN];
             const float4 B = q[(ph + QN - R + rr) % QN];
-            av[0] = A.x; av[1] = A.y; av[2] = A.z; av[3] = A.w;
-            bv[0] = B.x; bv[1] = B.y; bv[2] = B.z; bv[3] = B.w;
+            sum = add4({make_float2(A.x, A.y), make_float2(A.z, A.w)},
+                       {make_float2(B.x, B.y), make_float2(B.z, B.w)});
           }
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const float d = (av[c] + bv[c]) - (w[4 + c] + w[4 + c]);
-            acc[c] = p == 0 ? G.cf.cf[0] * d : __fmaf_rn(G.cf.cf[p], d, acc[c]);
-          }
+          const P4 d = add4(sum, nu2);
+          acc = p == 0 ? mul4(d, splat(G.cf.cf[0])) : fma4(splat(G.cf.cf[p]), d, acc);
         }
         const float4 v4 = *reinterpret_cast<const float4*>(vr + stage * kVSlot + r * TK + 4 * lane);
         const float4 s4 = *reinterpret_cast<const float4*>(sr + stage * kVSlot + r * TK + 4 * lane);
-        const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
-        float ss[4] = {s4.x, s4.y, s4.z, s4.w};
-        float o[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          if (i == G.src_i && j == G.src_j && k + c == G.src_k) ss[c] = ss[c] + amp;
-          float t = (w[4 + c] + w[4 + c]) - vv[c];
-          t = __fmaf_rn(G.cf.c1, acc[c], t);
-          o[c] = __fmaf_rn(G.cf.c2, ss[c], t);
+        P4 ss = {make_float2(s4.x, s4.y), make_float2(s4.z, s4.w)};
+        if (i == G.src_i && j == G.src_j && (unsigned)(G.src_k - k) < 4u) {
+          const int c = G.src_k - k;
+          if (c == 0) ss.a.x = ss.a.x + amp;
+          if (c == 1) ss.a.y = ss.a.y + amp;
+          if (c == 2) ss.b.x = ss.b.x + amp;
+          if (c == 3) ss.b.y = ss.b.y + amp;
         }
+        P4 t = add4(u2, {make_float2(-v4.x, -v4.y), make_float2(-v4.z, -v4.w)});
+        t = fma4(splat(G.cf.c1), acc, t);
+        const P4 x = fma4(splat(G.cf.c2), ss, t);
+        const float o[4] = {x.a.x, x.a.y, x.b.x, x.b.y};
         if (row_ok) {
           float* dst = vrow + (long long)i * g.si;
           if (k + 3 < g.zs) {

@@ -33,8 +33,11 @@
 // as an error code instead of a hung GPU.
 //
 // Arithmetic: the same operation sequence as the direct-load kernel and the
-// oracle's fma flavour (see st3d_kernels_simple.cu).
+// oracle's fma flavour (see st3d_kernels_simple.cu), on packed FP32 pairs
+// (add/fma.rn.f32x2, per component the scalar operations; the k pairs of odd
+// offset straddle register pairs and are added one point at a time).
 #include "st3d_internal.h"
+#include "st3d_p4.cuh"
 #include "st3d_tma.cuh"
 
 namespace st3d {
@@ -168,56 +171,60 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
           const float4 r4 = *reinterpret_cast<const float4*>(uc + 2 * kTmaKHalo + 4 * lane);
           const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w,
                                r4.x, r4.y, r4.z, r4.w};
-          float acc[4];
+          const P4 cu = {make_float2(c4.x, c4.y), make_float2(c4.z, c4.w)};
+          const P4 u2 = add4(cu, cu);
+          const P4 nu2 = {make_float2(-u2.a.x, -u2.a.y), make_float2(-u2.b.x, -u2.b.y)};
+          P4 acc;
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
             const int ax = pair_axis(P, p);
             const int rr = pair_r(P, p);
-            float a[4], b[4];
-            if (ax == 2) {
-#pragma unroll
-              for (int c = 0; c < 4; ++c) {
-                a[c] = w[4 + c - rr];
-                b[c] = w[4 + c + rr];
-              }
+            P4 sum;
+            if (ax == 2 && (rr & 1)) {
+              sum = {make_float2(w[4 - rr] + w[4 + rr], w[5 - rr] + w[5 + rr]),
+                     make_float2(w[6 - rr] + w[6 + rr], w[7 - rr] + w[7 + rr])};
+            } else if (ax == 2) {
+              sum = add4({make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])},
+                         {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])});
             } else if (ax == 1) {
               const float4 A = *reinterpret_cast<const float4*>(uc - rr * UKW + kTmaKHalo + 4 * lane);
               const float4 B = *reinterpret_cast<const float4*>(uc + rr * UKW + kTmaKHalo + 4 * lane);
-              a[0] = A.x; a[1] = A.y; a[2] = A.z; a[3] = A.w;
-              b[0] = B.x; b[1] = B.y; b[2] = B.z; b[3] = B.w;
+              sum = add4({make_float2(A.x, A.y), make_float2(A.z, A.w)},
+                         {make_float2(B.x, B.y), make_float2(B.z, B.w)});
             } else {
               const float4 A = q[(ph + 2 * QN - R - rr) % QN];
               const float4 B = q[(ph + QN - R + rr) % QN];
-              a[0] = A.x; a[1] = A.y; a[2] = A.z; a[3] = A.w;
-              b[0] = B.x; b[1] = B.y; b[2] = B.z; b[3] = B.w;
+              sum = add4({make_float2(A.x, A.y), make_float2(A.z, A.w)},
+                         {make_float2(B.x, B.y), make_float2(B.z, B.w)});
             }
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              const float pr = a[c] + b[c];
-              if (MODE == ST3D_MODE_REF) {
-                acc[c] = __fmaf_rn(cf.cf[p], pr, p == 0 ? cf.coef0 * w[4 + c] : acc[c]);
-              } else {
-                const float d = pr - (w[4 + c] + w[4 + c]);
-                acc[c] = p == 0 ? cf.cf[0] * d : __fmaf_rn(cf.cf[p], d, acc[c]);
-              }
+            if (MODE == ST3D_MODE_REF) {
+              acc = fma4(splat(cf.cf[p]), sum, p == 0 ? mul4(cu, splat(cf.coef0)) : acc);
+            } else {
+              const P4 d = add4(sum, nu2);
+              acc = p == 0 ? mul4(d, splat(cf.cf[0])) : fma4(splat(cf.cf[p]), d, acc);
             }
           }
           const float4 v4 = *reinterpret_cast<const float4*>(vr + stage * VSLOT + r * TK + 4 * lane);
           const float4 s4 = *reinterpret_cast<const float4*>(sr + stage * VSLOT + r * TK + 4 * lane);
-          const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
-          float ss[4] = {s4.x, s4.y, s4.z, s4.w};
-          float o[4];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            if (MODE == ST3D_MODE_REF) {
-              o[c] = __fmaf_rn(ss[c], acc[c], __fmaf_rn(-cf.K, w[4 + c], vv[c]));
-            } else {
-              if (i == src.i && j == src.j && k + c == src.k) ss[c] = ss[c] + src.amp;
-              float t = (w[4 + c] + w[4 + c]) - vv[c];
-              t = __fmaf_rn(cf.c1, acc[c], t);
-              o[c] = __fmaf_rn(cf.c2, ss[c], t);
+          const P4 vv = {make_float2(v4.x, v4.y), make_float2(v4.z, v4.w)};
+          P4 ss = {make_float2(s4.x, s4.y), make_float2(s4.z, s4.w)};
+          P4 x;
+          if (MODE == ST3D_MODE_REF) {
+            const P4 t = fma4(splat(-cf.K), cu, vv);
+            x = {__ffma2_rn(ss.a, acc.a, t.a), __ffma2_rn(ss.b, acc.b, t.b)};
+          } else {
+            if (i == src.i && j == src.j && (unsigned)(src.k - k) < 4u) {
+              const int c = src.k - k;
+              if (c == 0) ss.a.x = ss.a.x + src.amp;
+              if (c == 1) ss.a.y = ss.a.y + src.amp;
+              if (c == 2) ss.b.x = ss.b.x + src.amp;
+              if (c == 3) ss.b.y = ss.b.y + src.amp;
             }
+            P4 t = add4(u2, {make_float2(-vv.a.x, -vv.a.y), make_float2(-vv.b.x, -vv.b.y)});
+            t = fma4(splat(cf.c1), acc, t);
+            x = fma4(splat(cf.c2), ss, t);
           }
+          const float o[4] = {x.a.x, x.a.y, x.b.x, x.b.y};
           if (row_ok) {
             float* dst = vrow + (long long)i * g.si;
             if (k + 3 < g.zs) {
