@@ -163,8 +163,10 @@ def batch_key(grids, points, device=None):
 
 def batch_candidates():
     """Batch knobs: planes per work unit (shorter units balance the shared
-    queue, longer ones re-read fewer warm-up planes) and the schedule."""
-    return [{"ichunk": ic, "schedule": sch} for ic in (32, 64, 128) for sch in ("graph", "persistent")]
+    queue, longer ones re-read fewer warm-up planes; 512 is a whole column
+    of every grid up to 512 planes) and the schedule."""
+    return [{"ichunk": ic, "schedule": sch} for ic in (32, 64, 128, 256, 512)
+            for sch in ("graph", "persistent")]
 
 
 def measure_batch_device(grids, points, cand, dts=None, srcs=None, steps=20, warmup=3):

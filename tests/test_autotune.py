@@ -85,7 +85,8 @@ def test_tune_batch_picks_and_caches(tmp_path):
 
     def model(c):
         seen.append(c)
-        return {32: 3.0, 64: 2.0, 128: 2.5}[c["ichunk"]] - (0.1 if c["schedule"] == "graph" else 0.0)
+        return {32: 3.0, 64: 2.0, 128: 2.5, 256: 2.6, 512: 2.7}[c["ichunk"]] - \
+            (0.1 if c["schedule"] == "graph" else 0.0)
 
     r = autotune.tune_batch(grids, pts, cache=path, measure=model, device=DEV)
     assert r["opts"] == {"ichunk": 64, "schedule": "graph"}
