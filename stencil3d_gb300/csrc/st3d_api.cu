@@ -796,6 +796,15 @@ int check_device_status(st3d_ctx* c) {
 
 }  // namespace
 
+namespace st3d {
+// FP32 tiled tensor map over one field buffer (encode_map above), for the
+// batch kernel's own tile shapes.
+int encode_f32_box(CUtensorMap* m, void* base, const Layout& L, uint32_t box_k, uint32_t box_j,
+                   uint32_t kext, uint32_t jext) {
+  return encode_map(m, base, L, box_k, box_j, kext, jext);
+}
+}  // namespace st3d
+
 // ---------------------------------------------------------------------------
 // library
 // ---------------------------------------------------------------------------

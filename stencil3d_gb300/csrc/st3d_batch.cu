@@ -2,8 +2,8 @@
 // sizes and stencil orders (independent source shots) advancing together.
 //
 // One time step of every grid is one persistent launch: CTAs (at most
-// #SMs x resident) pull work items -- one (grid, 16-row x 128-point tile,
-// i-chunk) unit each -- from a device work queue (an atomic head over an item
+// #SMs x resident) pull work items -- one (grid, 16-row x 128-point or
+// 32-row x 64-point tile, i-chunk) unit each -- from a device work queue (an atomic head over an item
 // table ordered largest grid first), so small and large grids, 7-, 13- and
 // 25-point stencils share the GPU without a launch per grid.  The producer
 // warp of each CTA takes the next item, streams that grid's planes in with
@@ -31,6 +31,11 @@ namespace st3d {
 namespace {
 
 constexpr int kBTJ = 16;
+// Narrow tiles (32 rows x 64 points, each consumer warp serving two rows with
+// 16 lanes each) for grids whose k extent fits them better: the same 2048
+// points, v/s slots and warps per tile, a u slot that fits the wide one's.
+constexpr int kNTJ = 32;
+constexpr int kNTK = 64;
 constexpr int kBNV = 4;  // 4 stages: 241.5 against 237.8 Gpts/s with 3 on the 64-grid batch
 constexpr int kBRmax = 4;
 
@@ -43,6 +48,7 @@ struct BatchGrid {
   int src_i, src_j, src_k;
   int cur0;      // buffer holding u at the call's first step
   int map_base;  // index of the grid's 5 tensor maps: u over buf 0/1, v over buf 0/1, s
+  int narrow;    // tiles of kNTJ x kNTK instead of kBTJ x kTmaTK
 };
 
 struct BatchArgs {
@@ -73,23 +79,33 @@ size_t batch_smem_bytes() {
 }
 
 // The consumer side of one work unit (the single-grid kernel's consumer loop
-// for stencil P): nsteps pipeline stages starting at global stage h0.
+// for stencil P): nsteps pipeline stages starting at global stage h0.  Warp
+// w serves tile row w (wide tiles) or rows 2w and 2w + 1 with lanes 0-15 and
+// 16-31 (narrow tiles); `r` and `kl` are the lane's tile row and column.  The
+// tile shape is a run-time value so that one copy of the loop per order
+// serves both (two template copies spilled registers).
+static_assert((kNTK + 2 * kTmaKHalo) * (kNTJ + 2 * kBRmax) <= kUSlot && kNTK * kNTJ == kVSlot,
+              "narrow tile does not fit the slots");
 template <int P>
 __device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid& G, int gi, int unit,
                                              uint32_t h0, float* ur, float* vr, float* sr,
-                                             uint64_t* full, uint64_t* empty, int r, int lane) {
+                                             uint64_t* full, uint64_t* empty, int warp, int lane) {
   constexpr int R = (P == 25) ? 4 : (P == 13) ? 2 : 1;
   constexpr int QN = 2 * R + 1;
   constexpr int NP = npairs_of(P);
-  constexpr int TK = kTmaTK;
-  constexpr int UKW = kTmaUKW;
+  const bool narrow = G.narrow != 0;
+  const int TJ = narrow ? kNTJ : kBTJ;
+  const int TK = narrow ? kNTK : kTmaTK;
+  const int UKW = TK + 2 * kTmaKHalo;
+  const int r = narrow ? 2 * warp + (lane >> 4) : warp;
+  const int kl = narrow ? (lane & 15) : lane;
   const Geom& g = G.g;
   const int ic = unit / G.ntjk;
   const int rem = unit - ic * G.ntjk;
   const int jt = rem / G.ntk;
   const int kt = rem - jt * G.ntk;
-  const int j = jt * kBTJ + r;
-  const int k = kt * TK + 4 * lane;
+  const int j = jt * TJ + r;
+  const int k = kt * TK + 4 * kl;
   const int ia = ic * G.ichunk;
   const int ib = min(ia + G.ichunk, g.xs);
   const int nsteps = (ib - ia) + 2 * R;
@@ -110,13 +126,13 @@ __device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid
         atomicExch(a.status, (uint32_t)kDevTimeoutFull);
         return false;
       }
-      q[ph] = *reinterpret_cast<const float4*>(ur + (hh % kNU) * kUSlot + (r + R) * UKW + kTmaKHalo + 4 * lane);
+      q[ph] = *reinterpret_cast<const float4*>(ur + (hh % kNU) * kUSlot + (r + R) * UKW + kTmaKHalo + 4 * kl);
       if (n >= 2 * R) {
         const int i = ia + n - 2 * R;
         const float* uc = ur + ((hh - R) % kNU) * kUSlot + (r + R) * UKW;
         const float4 c4 = q[(ph + QN - R) % QN];
-        const float4 l4 = *reinterpret_cast<const float4*>(uc + 4 * lane);
-        const float4 r4 = *reinterpret_cast<const float4*>(uc + 2 * kTmaKHalo + 4 * lane);
+        const float4 l4 = *reinterpret_cast<const float4*>(uc + 4 * kl);
+        const float4 r4 = *reinterpret_cast<const float4*>(uc + 2 * kTmaKHalo + 4 * kl);
         const float w[12] = {l4.x, l4.y, l4.z, l4.w, c4.x, c4.y, c4.z, c4.w, r4.x, r4.y, r4.z, r4.w};
         const P4 cu = {make_float2(c4.x, c4.y), make_float2(c4.z, c4.w)};
         const P4 u2 = add4(cu, cu);
@@ -134,8 +150,8 @@ __device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid
             sum = add4({make_float2(w[4 - rr], w[5 - rr]), make_float2(w[6 - rr], w[7 - rr])},
                        {make_float2(w[4 + rr], w[5 + rr]), make_float2(w[6 + rr], w[7 + rr])});
           } else if (ax == 1) {
-            const float4 A = *reinterpret_cast<const float4*>(uc - rr * UKW + kTmaKHalo + 4 * lane);
-            const float4 B = *reinterpret_cast<const float4*>(uc + rr * UKW + kTmaKHalo + 4 * lane);
+            const float4 A = *reinterpret_cast<const float4*>(uc - rr * UKW + kTmaKHalo + 4 * kl);
+            const float4 B = *reinterpret_cast<const float4*>(uc + rr * UKW + kTmaKHalo + 4 * kl);
             sum = add4({make_float2(A.x, A.y), make_float2(A.z, A.w)},
                        {make_float2(B.x, B.y), make_float2(B.z, B.w)});
           } else {
@@ -147,8 +163,8 @@ __device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid
           const P4 d = add4(sum, nu2);
           acc = p == 0 ? mul4(d, splat(G.cf.cf[0])) : fma4(splat(G.cf.cf[p]), d, acc);
         }
-        const float4 v4 = *reinterpret_cast<const float4*>(vr + stage * kVSlot + r * TK + 4 * lane);
-        const float4 s4 = *reinterpret_cast<const float4*>(sr + stage * kVSlot + r * TK + 4 * lane);
+        const float4 v4 = *reinterpret_cast<const float4*>(vr + stage * kVSlot + r * TK + 4 * kl);
+        const float4 s4 = *reinterpret_cast<const float4*>(sr + stage * kVSlot + r * TK + 4 * kl);
         P4 ss = {make_float2(s4.x, s4.y), make_float2(s4.z, s4.w)};
         if (i == G.src_i && j == G.src_j && (unsigned)(G.src_k - k) < 4u) {
           const int c = G.src_k - k;
@@ -228,7 +244,8 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
       const int rem = unit - ic * G.ntjk;
       const int jt = rem / G.ntk;
       const int kt = rem - jt * G.ntk;
-      const int k0 = kt * kTmaTK, j0 = jt * kBTJ;
+      const int tk = G.narrow ? kNTK : kTmaTK, tj = G.narrow ? kNTJ : kBTJ;
+      const int k0 = kt * tk, j0 = jt * tj;
       const int ia = ic * G.ichunk;
       const int ib = min(ia + G.ichunk, G.g.xs);
       const int nsteps = (ib - ia) + 2 * R;
@@ -236,7 +253,7 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
       const CUtensorMap* umap = &a.maps[G.map_base + ub];
       const CUtensorMap* vmap = &a.maps[G.map_base + 2 + (ub ^ 1)];
       const CUtensorMap* smap = &a.maps[G.map_base + 4];
-      const uint32_t ubytes = (uint32_t)(kTmaUKW * (kBTJ + 2 * R) * 4);
+      const uint32_t ubytes = (uint32_t)((tk + 2 * kTmaKHalo) * (tj + 2 * R) * 4);
       const uint32_t vbytes = (uint32_t)(kVSlot * 4);
       for (int n = 0; n < nsteps; ++n, ++h) {
         const int stage = (int)(h % kBNV);
@@ -470,19 +487,41 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
     G.buf[1] = (float*)c->fld[1];
     G.P = o.points;
     G.R = c->R;
-    G.ntk = c->tma->ntk;
-    G.ntjk = c->tma->ntj * c->tma->ntk;
+    // tile shape: the one that pads the (j, k) plane less (wide on a tie)
+    const long long ys = grids[gi].ys, zs = grids[gi].zs;
+    const long long wide = (ys + kBTJ - 1) / kBTJ * kBTJ * ((zs + kTmaTK - 1) / kTmaTK * kTmaTK);
+    const long long thin = (ys + kNTJ - 1) / kNTJ * kNTJ * ((zs + kNTK - 1) / kNTK * kNTK);
+    G.narrow = thin < wide ? 1 : 0;
     G.ichunk = c->tma->ichunk;
-    G.units = c->tma->units;
+    if (G.narrow) {
+      const int ntj = (int)((ys + kNTJ - 1) / kNTJ);
+      G.ntk = (int)((zs + kNTK - 1) / kNTK);
+      G.ntjk = ntj * G.ntk;
+      G.units = G.ntjk * (int)((grids[gi].xs + G.ichunk - 1) / G.ichunk);
+    } else {
+      G.ntk = c->tma->ntk;
+      G.ntjk = c->tma->ntj * c->tma->ntk;
+      G.units = c->tma->units;
+    }
     G.src_i = c->opts.src_i;
     G.src_j = c->opts.src_j;
     G.src_k = c->opts.src_k;
     G.map_base = 5 * (int)gi;
-    maps[5 * gi + 0] = c->tma->umap[0];
-    maps[5 * gi + 1] = c->tma->umap[1];
-    maps[5 * gi + 2] = c->tma->vmap[0];
-    maps[5 * gi + 3] = c->tma->vmap[1];
-    maps[5 * gi + 4] = c->tma->vmap[2];
+    if (G.narrow) {
+      for (int f = 0; f < 3 && rc == ST3D_OK; ++f) {
+        if (f < 2)
+          rc = encode_f32_box(&maps[5 * gi + f], c->fld[f], c->L, kNTK + 2 * kTmaKHalo, kNTJ + 2 * c->R,
+                              kTmaKHalo, c->L.pj);
+        if (rc == ST3D_OK) rc = encode_f32_box(&maps[5 * gi + 2 + f], c->fld[f], c->L, kNTK, kNTJ, 0, 0);
+      }
+      if (rc != ST3D_OK) return cleanup(rc);
+    } else {
+      maps[5 * gi + 0] = c->tma->umap[0];
+      maps[5 * gi + 1] = c->tma->umap[1];
+      maps[5 * gi + 2] = c->tma->vmap[0];
+      maps[5 * gi + 3] = c->tma->vmap[1];
+      maps[5 * gi + 4] = c->tma->vmap[2];
+    }
     b->points += (uint64_t)grids[gi].xs * grids[gi].ys * grids[gi].zs;
   }
   // work items, the most expensive grids first (longest processing time

@@ -82,6 +82,13 @@ inline int tma_pick_ichunk(int xs, int tiles, int ctas, int R) {
   return best;
 }
 
+struct Layout;
+// FP32 tiled tensor map over one field buffer with a box of box_k x box_j
+// points; the valid extent is the row front pad + zs + kext along k and the
+// front rows + ys + jext along j (st3d_api.cu).
+int encode_f32_box(CUtensorMap* m, void* base, const Layout& L, uint32_t box_k, uint32_t box_j,
+                   uint32_t kext, uint32_t jext);
+
 inline size_t tma_smem_bytes(int tj, int nv, int R) {
   const size_t uslot = ((size_t)kTmaUKW * (tj + 2 * R) + 31) / 32 * 32 * 4;
   const size_t vslot = (size_t)kTmaTK * tj * 4;
