@@ -25,6 +25,9 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <cstring>
+#include <type_traits>
+
 #include "st3d_internal.h"
 
 namespace st3d {
@@ -120,6 +123,64 @@ __global__ void __launch_bounds__(kSimpleBX* kSimpleBY)
   }
 }
 
+// The same update with 16-byte accesses: a thread owns V = 16/sizeof(T)
+// consecutive points of a row (aligned: rows start on 128-byte boundaries),
+// takes u[k+V] with one more load, and walks its chunk of planes two at a
+// time so that more loads are in flight.  Rows carry at least 32 floats of
+// padding past zs, so the vector loads of a row's last points stay inside it.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_two_point_vec(Geom g, T coef0, T* __restrict__ v, const T* __restrict__ u, int ichunk) {
+  constexpr int V = 16 / sizeof(T);
+  using VT = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) * V;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (k >= g.zs || j >= g.ys) return;
+  const int i0 = blockIdx.z * ichunk;
+  const int i1 = min(i0 + ichunk, g.xs);
+  const long long row = g.org + (long long)j * g.sj + k;
+  for (int i = i0; i < i1; i += 2) {
+    const bool two = i + 1 < i1;
+    const long long x0 = row + (long long)i * g.si, x1 = x0 + g.si;
+    const VT a0 = __ldg(reinterpret_cast<const VT*>(u + x0));
+    const T n0 = __ldg(u + x0 + V);
+    VT a1;
+    T n1 = T(0);
+    if (two) {
+      a1 = __ldg(reinterpret_cast<const VT*>(u + x1));
+      n1 = __ldg(u + x1 + V);
+    }
+    T e0[V + 1], e1[V + 1];
+    memcpy(e0, &a0, sizeof a0);
+    e0[V] = n0;
+    if (two) {
+      memcpy(e1, &a1, sizeof a1);
+      e1[V] = n1;
+    }
+    T o0[V], o1[V];
+#pragma unroll
+    for (int c = 0; c < V; ++c) {
+      o0[c] = coef0 * (e0[c] + e0[c + 1]);
+      o1[c] = two ? coef0 * (e1[c] + e1[c + 1]) : T(0);
+    }
+    if (k + V <= g.zs) {
+      VT w0;
+      memcpy(&w0, o0, sizeof w0);
+      *reinterpret_cast<VT*>(v + x0) = w0;
+      if (two) {
+        VT w1;
+        memcpy(&w1, o1, sizeof w1);
+        *reinterpret_cast<VT*>(v + x1) = w1;
+      }
+    } else {
+      for (int c = 0; c < V && k + c < g.zs; ++c) {
+        v[x0 + c] = o0[c];
+        if (two) v[x1 + c] = o1[c];
+      }
+    }
+  }
+}
+
 template <typename T, int P, int MODE>
 cudaError_t launch_t(const Geom& g, const void* coefs, void* v, const void* u, const void* s,
                      const Source& src, int ichunk, cudaStream_t stream) {
@@ -128,7 +189,16 @@ cudaError_t launch_t(const Geom& g, const void* coefs, void* v, const void* u, c
   dim3 grid((g.zs + kSimpleBX - 1) / kSimpleBX, (g.ys + kSimpleBY - 1) / kSimpleBY,
             (g.xs + ichunk - 1) / ichunk);
   if constexpr (P == 2) {
-    k_two_point<T><<<grid, block, 0, stream>>>(g, cf.coef0, (T*)v, (const T*)u, ichunk);
+    // 16-byte accesses need 16-byte aligned rows (always: rows start on
+    // 128-byte boundaries) and a 16-byte aligned base
+    if (((uintptr_t)v | (uintptr_t)u) % 16 == 0) {
+      constexpr int V = 16 / sizeof(T);
+      dim3 vb(64, 4, 1);
+      dim3 vg((g.zs + 64 * V - 1) / (64 * V), (g.ys + 3) / 4, (g.xs + ichunk - 1) / ichunk);
+      k_two_point_vec<T><<<vg, vb, 0, stream>>>(g, cf.coef0, (T*)v, (const T*)u, ichunk);
+    } else {
+      k_two_point<T><<<grid, block, 0, stream>>>(g, cf.coef0, (T*)v, (const T*)u, ichunk);
+    }
   } else {
     T amp = sizeof(T) == 8 ? (T)src.amp_d : (T)src.amp;
     k_simple<T, P, MODE><<<grid, block, 0, stream>>>(g, cf, (T*)v, (const T*)u, (const T*)s,

@@ -246,3 +246,25 @@ def test_metrics_report_the_timed_region():
         assert m["energy_u"] == e2 and m["max_abs_u"] == em
         assert m["rel_l2"] == 0.0
         assert a.metrics()["rel_l2"] == -1.0
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+@pytest.mark.parametrize("grid,ichunk", [((7, 9, 13, 4, 4, 4), 3), ((5, 30, 67, 4, 4, 16), 64),
+                                         ((12, 17, 256, 4, 4, 4), 5), ((3, 4, 1, 4, 4, 4), 0)])
+def test_two_point_matches_oracle(dtype, grid, ichunk):
+    """stencil_2 (v = 0.5(u + u[k+1]), u's k halo supplying u[zs]) on the
+    16-byte-access kernel: ragged rows (zs not a multiple of the vector
+    width), odd plane counts per chunk, FP32 and FP64, bit for bit; halos of
+    v untouched."""
+    v, s, u = mode_r_inputs(grid, 77, dtype)
+    v0 = v.copy()
+    g = S.Grid(*grid)
+    with S.Stencil(g, 2, "ref", dtype, ichunk=ichunk) as st:
+        st.iterate_host(v, s, u, 3)
+    vf, sf, uf = mode_r_inputs(grid, 77, dtype)
+    O.iterate_ref(vf, sf, uf, grid, 2, 3, fma=True)
+    np.testing.assert_array_equal(O.interior(v, grid), O.interior(vf, grid))
+    mask = np.ones(v.shape, bool)
+    xs, ys, zs, xh, yh, zh = grid
+    mask[xh:xh + xs, yh:yh + ys, zh:zh + zs] = False
+    np.testing.assert_array_equal(v[mask], v0[mask])
