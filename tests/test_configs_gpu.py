@@ -8,7 +8,9 @@
   - 13 points, 1040^3, leapfrog wave with 8 seeded Gaussian blobs: two steps
     fused per pass equal plain steps bit for bit (device-side difference);
   - the 64-grid batch (axes U{64..320}, orders {7, 13, 25}): the graph
-    schedule equals the sequential one bit for bit on every grid.
+    schedule equals the sequential one bit for bit on every grid;
+  - 1264^3, the largest grid the reference's command line accepts, in FP32
+    (both kernels, known answer) and in the FP16 delta and pair forms.
 """
 import numpy as np
 import pytest
@@ -104,3 +106,27 @@ def test_largest_grid_the_reference_accepts(points):
             st.iterate(1)
             assert st.check(3.0) == 0
             assert st.check(2.0) == 1264 ** 3
+
+
+def test_largest_grid_in_16bit_storage():
+    """1264^3 in the FP16 delta form and its hi/lo pair form: word offsets run
+    past 2^31 in the 16-bit kernels, encoders and decoders.  Three steps of a
+    blob field stay within the forms' rounding of the FP32 run (device
+    reductions over every point)."""
+    g = S.Grid(1264, 1264, 1264, 4, 4, 4)
+    ctx = {}
+    try:
+        for storage in ("f32", "f16", "f16_hl"):
+            st = S.Stencil(g, 25, "wave", storage, dt=5e-4, src=(632, 632, 632))
+            ctx[storage] = st
+            st.fill(S.FIELD_U, S.FILL_BLOBS, 20251203, 8, 40.0)
+            st.fill(S.FIELD_V, S.FILL_BLOBS, 20251203, 8, 40.0)
+            st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
+            st.iterate(3)
+            st.synchronize()
+        for storage, bound in (("f16", 2e-3), ("f16_hl", 1e-4)):
+            d2, b2, dm, bm = ctx[storage].norms(S.FIELD_U, ctx["f32"], S.FIELD_U)
+            assert b2 > 0 and np.isfinite(d2) and (d2 / b2) ** 0.5 < bound, (storage, d2, b2)
+    finally:
+        for st in ctx.values():
+            st.close()
