@@ -16,6 +16,13 @@ to device and device to host copies inside the timed region.  The u, v and
 s fields of the default workload take 13.9 GB in the device layout, far more
 than the 129 MB L2, so no flush is needed between steps.
 
+Beside the headline the line carries: the 16-bit storage forms (``fp16``:
+FP16 and BF16 delta forms, the FP16 hi/lo pair form, FP16 + int8) with their
+error against an FP64 run every 100 steps over 1000 steps, and the guarded
+FP16 run that moves to a compensated form past half of a 1e-3 tolerance;
+the FP64 path; the 64-grid batch (sequential, persistent, graph, tuned);
+temporal blocking (1/2/4 fused steps); ``e2e``; ``cpu_baseline``.
+
 ``--impl reference`` times the CPU restatement of the path (the oracle; the
 reference's own compiled path where it runs on this machine) with every host
 core on the same workload, one full time step per step.
