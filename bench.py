@@ -79,6 +79,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batch-steps", type=int, default=500,
                    help="steps of the batching-form run: 64 seeded grids (0 to skip)")
+    p.add_argument("--batch-grids", type=int, default=64,
+                   help="grids of the batching-form run (the first n of the seeded list)")
     p.add_argument("--precision-forms", default="f16_hilo,f16_hl,f16,bf16",
                    help="16-bit storage forms timed and judged against FP64 ('' to skip)")
     p.add_argument("--guard-fallback", default="f16_hilo", choices=["f16_hilo", "f16_hl"],
@@ -269,15 +271,15 @@ def batch_specs(seed=SEED, n=64):
     return specs
 
 
-def batch_run(S, steps, warmup):
+def batch_run(S, steps, warmup, n=64):
     """Aggregate throughput of the batching form under each schedule."""
-    specs = batch_specs()
+    specs = batch_specs(n=n)
     grids = [S.Grid(xs, ys, zs, 4, 4, 4) for (xs, ys, zs), _, _ in specs]
     pts = [p for _, p, _ in specs]
     dts = [1e-3 if p == 7 else 5e-4 for p in pts]
     srcs = [s for _, _, s in specs]
     out = {"grids": len(specs), "steps": steps,
-           "workload": "64 grids, axes U{64..320}, orders {7,13,25}, FP32 wave, seeded sources"}
+           "workload": "%d grids, axes U{64..320}, orders {7,13,25}, FP32 wave, seeded sources" % n}
     with S.Batch(grids, pts, dt=dts, srcs=srcs) as b:
         for i in range(len(grids)):
             st = b.context(i)
@@ -545,7 +547,7 @@ def run_gb300(args, dist):
             result["fp16"][form]["l2_err_vs_fp64"] = acc[form][-1]["rel_l2"]
 
     if dist.rank == 0 and args.batch_steps > 0:
-        result["batch"] = batch_run(S, args.batch_steps, args.warmup)
+        result["batch"] = batch_run(S, args.batch_steps, args.warmup, args.batch_grids)
 
     tws = [w for w in args.temporal_workloads.split(",") if w]
     if dist.rank == 0 and tws:
