@@ -2,8 +2,8 @@
 // sizes and stencil orders (independent source shots) advancing together.
 //
 // One time step of every grid is one persistent launch: CTAs (at most
-// #SMs x resident) pull work items -- one (grid, 16-row x 128-point or
-// 32-row x 64-point tile, i-chunk) unit each -- from a device work queue (an atomic head over an item
+// #SMs x resident) pull work items -- one (grid, 12-row x 128-point or
+// 24-row x 64-point tile, i-chunk) unit each -- from a device work queue (an atomic head over an item
 // table ordered largest grid first), so small and large grids, 7-, 13- and
 // 25-point stencils share the GPU without a launch per grid.  The producer
 // warp of each CTA takes the next item, streams that grid's planes in with
@@ -30,13 +30,18 @@ namespace st3d {
 
 namespace {
 
-constexpr int kBTJ = 16;
-// Narrow tiles (32 rows x 64 points, each consumer warp serving two rows with
-// 16 lanes each) for grids whose k extent fits them better: the same 2048
+// Wide tiles of 12 rows x 128 points: 12 consumer warps and a producer, so a
+// thread may hold 128 registers (the loop serving three stencil orders and
+// two tile shapes spilled 196 bytes at the 96 of a 17-warp CTA); measured on
+// the 64-grid batch: 16 rows 290.8, 12 rows 335.9, with 6 stages 362.4,
+// 10 rows 312.5, 14 rows x 5 stages 364.9 Gpts/s.
+constexpr int kBTJ = 12;
+// Narrow tiles (24 rows x 64 points, each consumer warp serving two rows with
+// 16 lanes each) for grids whose k extent fits them better: the same 1536
 // points, v/s slots and warps per tile, a u slot that fits the wide one's.
-constexpr int kNTJ = 32;
+constexpr int kNTJ = 24;
 constexpr int kNTK = 64;
-constexpr int kBNV = 4;  // 4 stages: 241.5 against 237.8 Gpts/s with 3 on the 64-grid batch
+constexpr int kBNV = 6;  // pipeline stages (4 measured 335.9, 6 362.4, 8 359.8 Gpts/s)
 constexpr int kBRmax = 4;
 
 struct BatchGrid {
@@ -471,8 +476,8 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
   for (uint32_t gi = 0; gi < n; ++gi) {
     st3d_opts o = opts[gi];
     o.kernel = ST3D_KERNEL_TMA;
-    o.tile_j = kBTJ;
-    o.stages = kBNV;
+    o.tile_j = 16;  // the single-grid plan, used by the sequential schedule
+    o.stages = 4;
     o.temporal_block = 1;  // the batch steps one level at a time
     if (o.ichunk <= 0) o.ichunk = 64;  // smaller units balance the shared queue
     st3d_ctx* c = nullptr;
@@ -493,35 +498,23 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
     const long long thin = (ys + kNTJ - 1) / kNTJ * kNTJ * ((zs + kNTK - 1) / kNTK * kNTK);
     G.narrow = thin < wide ? 1 : 0;
     G.ichunk = c->tma->ichunk;
-    if (G.narrow) {
-      const int ntj = (int)((ys + kNTJ - 1) / kNTJ);
-      G.ntk = (int)((zs + kNTK - 1) / kNTK);
-      G.ntjk = ntj * G.ntk;
-      G.units = G.ntjk * (int)((grids[gi].xs + G.ichunk - 1) / G.ichunk);
-    } else {
-      G.ntk = c->tma->ntk;
-      G.ntjk = c->tma->ntj * c->tma->ntk;
-      G.units = c->tma->units;
-    }
+    const int tk = G.narrow ? kNTK : kTmaTK, tj = G.narrow ? kNTJ : kBTJ;
+    G.ntk = (int)((zs + tk - 1) / tk);
+    G.ntjk = (int)((ys + tj - 1) / tj) * G.ntk;
+    G.units = G.ntjk * (int)((grids[gi].xs + G.ichunk - 1) / G.ichunk);
     G.src_i = c->opts.src_i;
     G.src_j = c->opts.src_j;
     G.src_k = c->opts.src_k;
     G.map_base = 5 * (int)gi;
-    if (G.narrow) {
-      for (int f = 0; f < 3 && rc == ST3D_OK; ++f) {
-        if (f < 2)
-          rc = encode_f32_box(&maps[5 * gi + f], c->fld[f], c->L, kNTK + 2 * kTmaKHalo, kNTJ + 2 * c->R,
-                              kTmaKHalo, c->L.pj);
-        if (rc == ST3D_OK) rc = encode_f32_box(&maps[5 * gi + 2 + f], c->fld[f], c->L, kNTK, kNTJ, 0, 0);
-      }
-      if (rc != ST3D_OK) return cleanup(rc);
-    } else {
-      maps[5 * gi + 0] = c->tma->umap[0];
-      maps[5 * gi + 1] = c->tma->umap[1];
-      maps[5 * gi + 2] = c->tma->vmap[0];
-      maps[5 * gi + 3] = c->tma->vmap[1];
-      maps[5 * gi + 4] = c->tma->vmap[2];
+    // the grid's maps in the batch's tile shape: u (halo box) over buffers 0
+    // and 1, v (interior box) over 0 and 1, s
+    for (int f = 0; f < 3 && rc == ST3D_OK; ++f) {
+      if (f < 2)
+        rc = encode_f32_box(&maps[5 * gi + f], c->fld[f], c->L, tk + 2 * kTmaKHalo, tj + 2 * c->R,
+                            kTmaKHalo, c->L.pj);
+      if (rc == ST3D_OK) rc = encode_f32_box(&maps[5 * gi + 2 + f], c->fld[f], c->L, tk, tj, 0, 0);
     }
+    if (rc != ST3D_OK) return cleanup(rc);
     b->points += (uint64_t)grids[gi].xs * grids[gi].ys * grids[gi].zs;
   }
   // work items, the most expensive grids first (longest processing time
