@@ -747,7 +747,8 @@ int plan_tb(st3d_ctx* c, int sm_count) {
   const int T = c->opts.temporal_block, R = c->R;
   p->T = T;
   p->radius = R;
-  p->rows_out = 16 - 2 * (T - 1) * R;
+  p->rows = tb_rows(c->opts.points, T);
+  p->rows_out = p->rows - 2 * (T - 1) * R;
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
   if ((int)tb_smem_bytes(c->opts.points, T) > max_smem || p->rows_out < 1) {
@@ -770,10 +771,10 @@ int plan_tb(st3d_ctx* c, int sm_count) {
   int ok = ST3D_OK;
   for (int f : {0, 1, 3, 4}) {
     if (ok == ST3D_OK)
-      ok = encode_map(&p->umap[f], c->fld[f], c->L, kTmaUKW, 16 + 2 * R, kTmaKHalo, c->L.pj);
-    if (ok == ST3D_OK) ok = encode_map(&p->vmap[f], c->fld[f], c->L, kTmaTK, 16, 0, 0);
+      ok = encode_map(&p->umap[f], c->fld[f], c->L, kTmaUKW, p->rows + 2 * R, kTmaKHalo, c->L.pj);
+    if (ok == ST3D_OK) ok = encode_map(&p->vmap[f], c->fld[f], c->L, kTmaTK, p->rows, 0, 0);
   }
-  if (ok == ST3D_OK) ok = encode_map(&p->vmap[2], c->fld[2], c->L, kTmaTK, 16, 0, 0);
+  if (ok == ST3D_OK) ok = encode_map(&p->vmap[2], c->fld[2], c->L, kTmaTK, p->rows, 0, 0);
   if (ok != ST3D_OK) {
     delete p;
     return ok;

@@ -14,10 +14,10 @@
 // (the "v" of the leapfrog): U^{n-1} from its TMA tile for t = 1, the oldest
 // entry of level t-2's queue above that.
 //
-// Tiles shrink by R per level: one consumer warp per row of a 16-row level-1
-// tile (rows j0 - (T-1)R ..), 4 points per lane over 128 columns
-// (k0 - 4 .. k0 + 123); the pass writes the 16 - 2(T-1)R middle rows and the
-// 120 columns k0 .. k0 + 119.  Level 1 is exact over its whole tile (the
+// Tiles shrink by R per level: one consumer warp per row of a level-1 tile
+// of tb_rows(P, T) rows (rows j0 - (T-1)R ..; 20 for 7 points T=2, else 16),
+// 4 points per lane over 128 columns (k0 - 4 .. k0 + 123); the pass writes
+// the rows - 2(T-1)R middle rows and the 120 columns k0 .. k0 + 119.  Level 1 is exact over its whole tile (the
 // level-0 TMA tile carries R rows and 4 columns of halo); a level above reads
 // zeros beyond its tile's edge, so level t is exact in all but (t-1)R rows
 // and columns at either edge, which bounds (T-1)R by the 4 spare columns:
@@ -42,7 +42,6 @@ namespace st3d {
 
 namespace {
 
-constexpr int kRows = 16;       // level-1 rows per tile = consumer warps
 constexpr int kCols = 128;      // level columns per tile (32 lanes x 4)
 constexpr int kOutCols = 120;   // columns written per tile
 constexpr int kW = kCols + 8;   // smem row width (4 floats of pad either side)
@@ -67,6 +66,7 @@ struct RadTB {
 template <int P, int T, int NV>
 struct TbShape {
   static constexpr int R = RadTB<P>::value;
+  static constexpr int kRows = tb_rows(P, T);  // level-1 rows per tile = consumer warps
   static constexpr int QN = 2 * R + 1;
   static constexpr int NU = NV + R;                       // level-0 ring (TMA u tiles)
   static constexpr int NS = NV + (T - 1) * R;             // s ring (kept for the later levels)
@@ -81,12 +81,13 @@ struct TbShape {
 };
 
 template <int P, int T, int NV>
-__global__ void __launch_bounds__((kRows + 1) * 32, 1)
+__global__ void __launch_bounds__((tb_rows(P, T) + 1) * 32, 1)
     k_tb(const __grid_constant__ CUtensorMap umap, const __grid_constant__ CUtensorMap vmap,
          const __grid_constant__ CUtensorMap smap, const TbArgs a) {
   using S = TbShape<P, T, NV>;
   constexpr int R = S::R;
   constexpr int QN = S::QN;
+  constexpr int kRows = S::kRows;
   constexpr int NP = npairs_of(P);
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float* ur = reinterpret_cast<float*>(smem_raw);
@@ -317,8 +318,9 @@ cudaError_t launch_pt(const TbPlan& pl, const TbArgs& a, const CUtensorMap& u, c
   const size_t smem = Sh::smem();
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, (kRows + 1) * 32, smem);
-  kern<<<pl.grid, (kRows + 1) * 32, smem, stream>>>(u, v, s, a);
+  if (occ) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, (Sh::kRows + 1) * 32, smem);
+  if (pl.rows != Sh::kRows) return cudaErrorInvalidConfiguration;  // maps built for another height
+  kern<<<pl.grid, (Sh::kRows + 1) * 32, smem, stream>>>(u, v, s, a);
   return cudaGetLastError();
 }
 

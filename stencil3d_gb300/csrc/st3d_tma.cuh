@@ -48,11 +48,19 @@ struct Tma16Plan {
 };
 
 // Plan of the temporally blocked kernel (st3d_kernels_tb.cu): T fused
-// steps, 16-row level-1 tiles writing rows_out = 16 - 2(T-1)R rows and 120
-// columns; tensor maps over the four state buffers (0, 1, 3, 4) and s (2):
-// umap is the plain kernel's halo box, vmap its interior box.
+// steps, level-1 tiles of tb_rows(points, T) rows writing rows_out =
+// rows - 2(T-1)R rows and 120 columns; tensor maps over the four state
+// buffers (0, 1, 3, 4) and s (2): umap the halo box (kTmaUKW x rows+2R), vmap
+// the interior box (kTmaTK x rows).  The kernel's transaction byte counts
+// assume these boxes, so plan and kernel take the height from this one
+// function.  7 points T=2 runs 20 rows (595 against 544 Gpts/s with 16 at
+// 1024^3, the same bits); 7 points T=4 does not fit in shared memory with
+// 20, and 13 points T=2 ran slower there (372 against 411 Gpts/s).
+__host__ __device__ constexpr int tb_rows(int points, int T) {
+  return (points == 7 && T == 2) ? 20 : 16;
+}
 struct TbPlan {
-  int T = 2, radius = 0, rows_out = 0;
+  int T = 2, radius = 0, rows = 16, rows_out = 0;
   int ichunk = 0, ntj = 0, ntk = 0, nti = 0, units = 0;
   int grid = 0;
   uint64_t timeout_ns = 4000000000ull;
