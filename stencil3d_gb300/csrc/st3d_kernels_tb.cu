@@ -15,7 +15,7 @@
 // entry of level t-2's queue above that.
 //
 // Tiles shrink by R per level: one consumer warp per row of a level-1 tile
-// of tb_rows(P, T) rows (rows j0 - (T-1)R ..; 20 for 7 points T=2, else 16),
+// of tb_rows(P, T) rows (rows j0 - (T-1)R ..; 26 for 7 points T=2, else 18),
 // 4 points per lane over 128 columns (k0 - 4 .. k0 + 123); the pass writes
 // the rows - 2(T-1)R middle rows and the 120 columns k0 .. k0 + 119.  Level 1 is exact over its whole tile (the
 // level-0 TMA tile carries R rows and 4 columns of halo); a level above reads

@@ -53,14 +53,17 @@ struct Tma16Plan {
 // buffers (0, 1, 3, 4) and s (2): umap the halo box (kTmaUKW x rows+2R), vmap
 // the interior box (kTmaTK x rows).  The kernel's transaction byte counts
 // assume these boxes, so plan and kernel take the height from this one
-// function.  7 points T=2 runs 20 rows (595 against 544 Gpts/s with 16 at
-// 1024^3, the same bits); 7 points T=4 does not fit in shared memory with
-// 20, and 13 points T=2 ran slower there (372 against 411 Gpts/s).
+// function.  Taller tiles recompute fewer halo rows per written row and run
+// more consumer warps, up to the register and shared-memory limits: 7 points
+// T=2 runs 26 rows (27 warps, 67 registers; 629 against 544 Gpts/s with 16
+// at 1024^3, the same bits), T=4 18 rows (568 against 531; 20 rows do not
+// fit in shared memory), 13 points T=2 18 rows (452 against 411; 20 rows cap
+// the registers at 80 and spill, 372).
 __host__ __device__ constexpr int tb_rows(int points, int T) {
-  return (points == 7 && T == 2) ? 20 : 16;
+  return (points == 7 && T == 2) ? 26 : 18;
 }
 struct TbPlan {
-  int T = 2, radius = 0, rows = 16, rows_out = 0;
+  int T = 2, radius = 0, rows = 0, rows_out = 0;
   int ichunk = 0, ntj = 0, ntk = 0, nti = 0, units = 0;
   int grid = 0;
   uint64_t timeout_ns = 4000000000ull;
