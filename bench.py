@@ -354,6 +354,7 @@ def temporal_run(S, workloads, steps, warmup, peak):
             entry = {"value": pts * steps / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
                      "ms_per_step": ms / steps, "launches": int(launches),
                      "bytes_per_point_step": info.bytes_per_point,
+                     "tile_rows": int(info.tb_tile_j or info.tile_j),
                      "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
                                   "frac": ach / peak}}
             if ref is None:

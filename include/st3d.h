@@ -156,7 +156,8 @@ typedef struct st3d_info {
   double flops_per_point;     /* reference FLOPS_PER_STENCIL (config.h:67-91) */
   int32_t tile_j, tile_k, ichunk, temporal_block;
   int32_t host_path;          /* st3d_host_path of the last upload or download */
-  int32_t reserved[7];
+  int32_t tb_tile_j;          /* rows of a temporally blocked pass's level-1 tile; 0 = none */
+  int32_t reserved[6];
 } st3d_info;
 
 typedef struct st3d_ctx st3d_ctx;

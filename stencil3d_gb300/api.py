@@ -61,7 +61,8 @@ class Info(C.Structure):
                 ("kernel", C.c_int32), ("radius", C.c_int32),
                 ("bytes_per_point", C.c_double), ("flops_per_point", C.c_double),
                 ("tile_j", C.c_int32), ("tile_k", C.c_int32), ("ichunk", C.c_int32),
-                ("temporal_block", C.c_int32), ("host_path", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("temporal_block", C.c_int32), ("host_path", C.c_int32), ("tb_tile_j", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class Metrics(C.Structure):

@@ -1163,6 +1163,7 @@ int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
   info->ichunk = c->tma ? c->tma->ichunk : c->tma16 ? c->tma16->ichunk : c->ichunk;
   info->temporal_block = c->opts.temporal_block;
   info->host_path = c->host_path;
+  info->tb_tile_j = c->tb ? c->tb->rows : 0;
   return ST3D_OK;
 }
 

@@ -112,3 +112,14 @@ def test_nonzero_halo_is_refused():
         with pytest.raises(S.St3dError) as e:
             st.upload(v, s, u)
         assert e.value.status == S.api.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("points,T,rows", [(7, 2, 26), (7, 4, 18), (13, 2, 18), (7, 1, 0)])
+def test_fused_tile_height_is_reported(points, T, rows):
+    """st3d_info.tb_tile_j: the level-1 rows of a fused pass's tile (the
+    height the plan's tensor maps and the kernel share), 0 without fusion."""
+    g = S.Grid(40, 60, 130, 4, 4, 4)
+    with S.Stencil(g, points, "wave", "f32", kernel="tma", temporal_block=T, dt=5e-4) as st:
+        info = st.info()
+        assert info.temporal_block == T
+        assert info.tb_tile_j == rows
