@@ -63,6 +63,12 @@ struct RadTB {
   static constexpr int value = (P == 13) ? 2 : 1;
 };
 
+// Pipeline stages: 13 points T=2 on 18 rows has room in shared memory for a
+// fourth (203 KB; 460 against 453 Gpts/s at 1024^3 with 3); the 7-point
+// tiles fill it with 3.
+template <int P, int T>
+constexpr int tb_stages() { return P == 13 ? 4 : 3; }
+
 template <int P, int T, int NV>
 struct TbShape {
   static constexpr int R = RadTB<P>::value;
@@ -313,8 +319,8 @@ __global__ void __launch_bounds__((tb_rows(P, T) + 1) * 32, 1)
 template <int P, int T>
 cudaError_t launch_pt(const TbPlan& pl, const TbArgs& a, const CUtensorMap& u, const CUtensorMap& v,
                       const CUtensorMap& s, cudaStream_t stream, int* occ) {
-  using Sh = TbShape<P, T, 3>;
-  auto kern = k_tb<P, T, 3>;
+  using Sh = TbShape<P, T, tb_stages<P, T>()>;
+  auto kern = k_tb<P, T, tb_stages<P, T>()>;
   const size_t smem = Sh::smem();
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -335,9 +341,9 @@ cudaError_t dispatch_tb(int points, int T, const TbPlan& pl, const TbArgs& a, co
 }  // namespace
 
 size_t tb_smem_bytes(int points, int T) {
-  if (points == 7 && T == 2) return TbShape<7, 2, 3>::smem();
-  if (points == 7 && T == 4) return TbShape<7, 4, 3>::smem();
-  if (points == 13 && T == 2) return TbShape<13, 2, 3>::smem();
+  if (points == 7 && T == 2) return TbShape<7, 2, tb_stages<7, 2>()>::smem();
+  if (points == 7 && T == 4) return TbShape<7, 4, tb_stages<7, 4>()>::smem();
+  if (points == 13 && T == 2) return TbShape<13, 2, tb_stages<13, 2>()>::smem();
   return 0;
 }
 
