@@ -353,7 +353,8 @@ int copy_field_strided(st3d_ctx* c, void* dev, void* host, bool to_device, bool 
 // The device address of a host array the kernels may read and write
 // directly: pinned (cudaMallocHost, cudaHostAlloc, cudaHostRegister) and
 // lying inside one allocation; nullptr otherwise (pageable memory, or a range
-// the CUDA runtime does not report as one pinned range), and the transfer then goes through staging.
+// the CUDA runtime does not report as one pinned range), and the transfer
+// then goes through staging.
 void* direct_view(const void* host, size_t bytes) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
