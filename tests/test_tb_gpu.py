@@ -44,7 +44,7 @@ def _run(grid, points, T, steps, v, s, u, src, dt=5e-4, **kw):
 
 @pytest.mark.parametrize("points,T", DEPTHS)
 @pytest.mark.parametrize("grid", [(21, 37, 250, 4, 4, 4), (5, 9, 17, 4, 4, 4),
-                                  (40, 30, 123, 4, 4, 8)])
+                                  (40, 30, 123, 4, 4, 8), (17, 48, 121, 4, 4, 4)])
 def test_fused_equals_plain_steps(points, T, grid):
     v, s, u = _inputs(grid, 11 + points)
     xs, ys, zs = grid[:3]
