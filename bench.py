@@ -58,7 +58,16 @@ WORKLOADS = {
 }
 # fused steps per pass served for each stencil order
 TB_DEPTHS = {7: (1, 2, 4), 13: (1, 2)}
+# timed steps of a temporal-blocking workload that has a stated run length:
+# the 13-point 1040^3 configuration runs 2000 steps at every depth
+TB_STEPS = {"wave13_1040": 2000}
+# the smaller benchmark configurations, each at its stated run length, FP32
+# plain steps of the wave form (the 256^3 and 528^3 runs of the reference's
+# host driver)
+CONFIG_RUNS = (("wave7_256", 20), ("wave25_528", 200))
 SEED = 20251203
+# CUDA device of this replica (LOCAL_RANK under torchrun)
+DEVICE = -1
 
 
 def parse():
@@ -90,7 +99,12 @@ def parse():
     p.add_argument("--temporal-workloads", default="wave7_1024,wave13_1040",
                    help="workloads timed with 1, 2 and 4 fused steps per pass ('' to skip)")
     p.add_argument("--temporal-steps", type=int, default=40,
-                   help="timed steps of each temporal-blocking run (a multiple of 4)")
+                   help="timed steps of each temporal-blocking run without a stated run length "
+                        "(a multiple of 4; wave13_1040 runs its 2000)")
+    p.add_argument("--mode-r-steps", type=int, default=20,
+                   help="timed steps of the mode R (reference update) run of the workload (0: skip)")
+    p.add_argument("--no-configs", dest="configs", action="store_false",
+                   help="skip the smaller benchmark configurations (wave7_256, wave25_528)")
     return p.parse_args()
 
 
@@ -171,6 +185,7 @@ def profile_traffic(kernel_tag, workload):
 
 # --------------------------------------------------------------------------
 def make_stencil(S, wl, storage="f32", kernel="auto", temporal_block=1, **kw):
+    kw.setdefault("device", DEVICE)
     points, xs, ys, zs, halo, dt, init = WORKLOADS[wl]
     g = S.Grid(xs, ys, zs, halo, halo, halo)
     st = S.Stencil(g, points, "wave", storage, kernel=kernel, dt=dt,
@@ -211,7 +226,7 @@ def accuracy_run(S, wl, steps, kernel, storages, guard_tol=1e-3, fallback="f16_h
     guard = None
     if guard_tol:
         guard = GuardedWave(ref_g, points, tol=guard_tol, fallback=fallback, dt=dt,
-                            src=(xs // 2, ys // 2, zs // 2))
+                            src=(xs // 2, ys // 2, zs // 2), device=DEVICE)
         init_fields(S, guard, init)
         guard_s = 0.0
     # The FP64 run advances in chunks of `every`: the guarded run is checked
@@ -280,7 +295,7 @@ def batch_run(S, steps, warmup, n=64):
     srcs = [s for _, _, s in specs]
     out = {"grids": len(specs), "steps": steps,
            "workload": "%d grids, axes U{64..320}, orders {7,13,25}, FP32 wave, seeded sources" % n}
-    with S.Batch(grids, pts, dt=dts, srcs=srcs) as b:
+    with S.Batch(grids, pts, dt=dts, srcs=srcs, device=DEVICE) as b:
         for i in range(len(grids)):
             st = b.context(i)
             st.fill(S.FIELD_U, S.FILL_BLOBS, SEED + i, 4, 12.0)
@@ -333,10 +348,11 @@ def temporal_run(S, workloads, steps, warmup, peak):
     pass over HBM (temporal blocking), and the fused result's agreement with
     plain steps (bitwise: max |difference| of u after the run)."""
     out = {}
-    steps = max(4, steps - steps % 4)
     for wl in workloads:
         points = WORKLOADS[wl][0]
-        res = {"steps": steps}
+        n = TB_STEPS.get(wl, steps)
+        n = max(4, n - n % 4)
+        res = {"steps": n}
         ref = None
         for T in TB_DEPTHS.get(points, (1,)):
             g, st = make_stencil(S, wl, "f32", "tma", temporal_block=T)
@@ -345,14 +361,14 @@ def temporal_run(S, workloads, steps, warmup, peak):
             st.synchronize()
             l0 = st.info().launches
             st.timer_start()
-            st.iterate(steps)
+            st.iterate(n)
             ms = st.timer_stop()
             st.synchronize()
             launches = st.info().launches - l0
             pts = g.gvol
-            ach = info.bytes_per_point * pts * steps / (ms * 1e-3) / 1e9
-            entry = {"value": pts * steps / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
-                     "ms_per_step": ms / steps, "launches": int(launches),
+            ach = info.bytes_per_point * pts * n / (ms * 1e-3) / 1e9
+            entry = {"value": pts * n / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+                     "ms_per_step": ms / n, "launches": int(launches),
                      "bytes_per_point_step": info.bytes_per_point,
                      "tile_rows": int(info.tb_tile_j or info.tile_j),
                      "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
@@ -370,6 +386,98 @@ def temporal_run(S, workloads, steps, warmup, peak):
             if isinstance(e, dict):
                 e["speedup_vs_T1"] = e["value"] / base
         out[wl] = res
+    return out
+
+
+def mode_r_run(S, wl, steps, warmup, peak):
+    """The reference's own update (mode R: stencil_25_ref_1, stencil_25.h:75-95
+    for 25 points) on the workload's grid, FP32: seeded u, v ~ U[-1, 1) and
+    s ~ U[0.5, 1.5) (the fields of the parity tests), u and s fixed, v
+    accumulating; one launch per step, CUDA events on the context's stream."""
+    points, xs, ys, zs, halo, dt, init = WORKLOADS[wl]
+    g = S.Grid(xs, ys, zs, halo, halo, halo)
+    with S.Stencil(g, points, "ref", "f32", device=DEVICE) as st:
+        st.fill(S.FIELD_U, S.FILL_UNIFORM, SEED, -1.0, 1.0)
+        st.fill(S.FIELD_V, S.FILL_UNIFORM, SEED + 1, -1.0, 1.0)
+        st.fill(S.FIELD_S, S.FILL_UNIFORM, SEED + 2, 0.5, 1.5)
+        info = st.info()
+        st.iterate(warmup)
+        st.synchronize()
+        l0 = st.info().launches
+        st.timer_start()
+        st.iterate(steps)
+        ms = st.timer_stop()
+        st.synchronize()
+        launches = st.info().launches - l0
+    value = g.gvol * steps / (ms * 1e-3) / 1e9
+    ach = info.bytes_per_point * g.gvol / (ms / max(1, launches) * 1e-3) / 1e9
+    return {"workload": "%s, mode R (the reference's update), seeded u, v ~ U[-1,1), "
+                        "s ~ U[0.5,1.5)" % wl,
+            "value": value, "unit": "Gpts/s", "steps": steps, "ms_per_step": ms / steps,
+            "launches": int(launches), "kernel": "k_tma<%d,ref>" % points,
+            "parity": "bit-exact to the oracle's fused flavour, <= 1e-5 relative L2 from the "
+                      "reference order (tests/test_configs_gpu.py, 20 steps at 1024^3)",
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": ach / peak, "bytes_per_point": info.bytes_per_point}}
+
+
+def config_runs(S, warmup, peak):
+    """The smaller benchmark configurations at their stated run lengths: the
+    plain FP32 wave steps, Gpts/s and the fraction of the HBM roofline."""
+    out = {}
+    for wl, steps in CONFIG_RUNS:
+        g, st = make_stencil(S, wl, "f32", "auto")
+        try:
+            info = st.info()
+            st.iterate(warmup)
+            st.synchronize()
+            st.timer_start()
+            st.iterate(steps)
+            ms = st.timer_stop()
+            st.synchronize()
+        finally:
+            st.close()
+        ach = info.bytes_per_point * g.gvol * steps / (ms * 1e-3) / 1e9
+        out[wl] = {"value": g.gvol * steps / (ms * 1e-3) / 1e9, "unit": "Gpts/s", "steps": steps,
+                   "ms_per_step": ms / steps, "fields_gb": round(3 * g.gsize * 4 / 1e9, 3),
+                   "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak}}
+    return out
+
+
+def _r(x, n=4):
+    """x rounded to n significant digits (None stays None)."""
+    if x is None:
+        return None
+    return float("%.*g" % (n, x))
+
+
+def summary_of(result):
+    """The figures a reader needs first, in one short object: the FP32
+    headline, mode R, each 16-bit form (Gpts/s, speed-up over FP32, roofline
+    fraction, relative L2 against FP64 after the accuracy run), the batch,
+    temporal blocking per depth and the smaller configurations."""
+    out = {"fp32": [_r(result["value"]), _r(result["roofline"]["frac"], 3),
+                    _r(result.get("l2_err_fp32_vs_fp64"), 3)],
+           "cols": "[Gpts/s, x FP32, HBM frac, rel L2 vs FP64 after the accuracy run]"}
+    if result.get("mode_r"):
+        out["mode_r"] = [_r(result["mode_r"]["value"]), _r(result["mode_r"]["roofline"]["frac"], 3)]
+    for form, e in (result.get("fp16") or {}).items():
+        if form == "f16_guarded":
+            out[form] = [_r(e.get("value")), None, None, _r(e.get("l2_err_vs_fp64"), 3)]
+            continue
+        out[form] = [_r(e["value"]), _r(e["speedup_vs_fp32"], 3), _r(e["roofline"]["frac"], 3),
+                     _r(e.get("l2_err_vs_fp64"), 3)]
+    b = result.get("batch")
+    if b:
+        out["batch"] = {"seq": _r(b["sequential"]["value"]), "persistent": _r(b["persistent"]["value"]),
+                        "graph": _r(b["graph"]["value"]), "graph_vs_seq": _r(b["graph_vs_sequential"], 3)}
+    for wl, r in (result.get("temporal_blocking") or {}).items():
+        out["tb_" + wl] = {k: _r(e["value"]) for k, e in r.items() if isinstance(e, dict)}
+        out["tb_" + wl]["steps"] = r["steps"]
+    for wl, e in (result.get("configs") or {}).items():
+        out[wl] = [_r(e["value"]), _r(e["roofline"]["frac"], 3)]
+    if result.get("e2e"):
+        out["e2e"] = _r(result["e2e"]["value"])
     return out
 
 
@@ -451,7 +559,9 @@ def host_threads():
 
 # --------------------------------------------------------------------------
 def run_gb300(args, dist):
+    global DEVICE
     import stencil3d_gb300 as S
+    DEVICE = dist.local_rank  # one replica per GPU
     points, xs, ys, zs, halo, dt, init = WORKLOADS[args.workload]
     g, st = make_stencil(S, args.workload, "f32", args.kernel)
     info = st.info()
@@ -547,6 +657,12 @@ def run_gb300(args, dist):
             result["fp16"][form]["accuracy_vs_fp64"] = acc[form]
             result["fp16"][form]["l2_err_vs_fp64"] = acc[form][-1]["rel_l2"]
 
+    if dist.rank == 0 and args.mode_r_steps > 0:
+        result["mode_r"] = mode_r_run(S, args.workload, args.mode_r_steps, args.warmup, peak)
+
+    if dist.rank == 0 and args.configs:
+        result["configs"] = config_runs(S, args.warmup, peak)
+
     if dist.rank == 0 and args.batch_steps > 0:
         result["batch"] = batch_run(S, args.batch_steps, args.warmup, args.batch_grids)
 
@@ -573,6 +689,9 @@ def run_gb300(args, dist):
         result["cpu_baseline"] = cpu_wave_sample(args.workload, u_host, v_host,
                                                  args.cpu_seconds, host_threads())
     if dist.rank == 0:
+        # last key of the line: the short summary stays inside any tail of
+        # the output a reader keeps
+        result["summary"] = summary_of(result)
         print(json.dumps(result), flush=True)
 
 
@@ -606,7 +725,10 @@ def run_reference(args, dist):
     el = time.perf_counter() - t0
     value = xs * ys * zs * timed / el / 1e9
     threads = host_threads()
-    kind = "reference" if O.ref_available(points) else "port"
+    # the wave form has no reference code: what runs is always the oracle's
+    # C restatement (kind "port"), whose mode R is pinned bit for bit to the
+    # reference's compiled path
+    kind = "port"
     sample = ("%d full leapfrog steps of %s on the CPU restatement (oracle), OpenMP %d threads"
               % (timed, args.workload, threads))
     print(json.dumps({
@@ -617,13 +739,12 @@ def run_reference(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "points": points, "grid": [xs, ys, zs],
                    "halo": halo, "form": "leapfrog wave", "dt": dt},
-        "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": threads, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": "the reference has no wave form; its CPU path restated in C (oracle/st3d_oracle.c, "
-                "pinned bit-exact to the reference's mode R) runs the same update" +
-                ("" if kind == "port" else "; reference library also present"),
+                "pinned bit-exact to the reference's mode R) runs the same update",
     }), flush=True)
 
 

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define ST3D_ABI_VERSION 1
+#define ST3D_ABI_VERSION 2
 
 typedef enum st3d_status {
   ST3D_OK = 0,
@@ -140,7 +140,12 @@ typedef struct st3d_opts {
   int32_t ichunk;                    /* planes per work unit along i; 0 = automatic */
   int32_t stages;                    /* pipeline stages of the TMA kernels; 0 = automatic */
   int32_t host_path;                 /* st3d_host_path of FP32/FP64 uploads and downloads */
-  int32_t reserved[6];
+  /* CUDA device ordinal the context runs on (one replica per GPU); -1, the
+   * st3d_default_opts value, takes the calling thread's current device.  Every
+   * entry point of the context makes it current for the call and restores the
+   * caller's device afterwards. */
+  int32_t device;
+  int32_t reserved[5];
 } st3d_opts;
 
 typedef struct st3d_info {
@@ -157,7 +162,8 @@ typedef struct st3d_info {
   int32_t tile_j, tile_k, ichunk, temporal_block;
   int32_t host_path;          /* st3d_host_path of the last upload or download */
   int32_t tb_tile_j;          /* rows of a temporally blocked pass's level-1 tile; 0 = none */
-  int32_t reserved[6];
+  int32_t device;             /* CUDA device ordinal of the context (st3d_plan: opts.device) */
+  int32_t reserved[5];
 } st3d_info;
 
 typedef struct st3d_ctx st3d_ctx;
@@ -232,7 +238,17 @@ int st3d_iterate(st3d_ctx* ctx, uint32_t iterations);
  * in mode W, u as well: u is then written although ITERATE declares it
  * const); synchronize. */
 int st3d_iterate_host(st3d_ctx* ctx, void* v, const void* s, void* u, uint32_t iterations);
+/* Waits for the context's stream; ST3D_ERR_TIMEOUT if a bounded device-side
+ * wait of a kernel gave up since the last call (the kernel then returned
+ * early and its results are void; the status word is cleared and the
+ * context stays usable). */
 int st3d_synchronize(st3d_ctx* ctx);
+/* Diagnostics: writes `code` into the context's device status word on its
+ * stream, as a kernel's bounded wait does when it gives up, so that the
+ * error path of st3d_synchronize (ST3D_ERR_TIMEOUT, then a usable context)
+ * can be exercised without a device wait running out.  No counterpart in
+ * the reference, which has no device waits.  code 0 clears the word. */
+int st3d_inject_device_status(st3d_ctx* ctx, uint32_t code);
 
 /* Device-side initialisation of one field (st3d_fill_kind); replaces
  * init_arrays (iterators.cpp:292-301) for ST3D_FILL_CONST. */
@@ -255,9 +271,12 @@ int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]);
  * st3d_norms' out; the work is enqueued on `stream` (a cudaStream_t, NULL for
  * the legacy default stream) and nothing is synchronised.  Partial sums live
  * in a 128 KiB array inside the library image: at most 4096 planes along i
- * (larger grids are rejected with ST3D_ERR_INVALID), calls that overlap on
- * the GPU race on it and must be serialised, and the first call on a device
- * looks up the array's address, so make it before any stream capture. */
+ * (larger grids are rejected with ST3D_ERR_INVALID, as is a grid beyond the
+ * limits every entry point applies: axes <= 2^24, halos <= 64/64/4096),
+ * calls that overlap on the GPU race on it and must be serialised, and the
+ * first call on a device looks up the array's address, so make it before any
+ * stream capture.  A cudaDeviceReset (a new context on the device) makes the
+ * next call look the address up again: make that call outside capture too. */
 int st3d_norms_noalloc(const st3d_grid_desc* grid, const void* a, int storage_a, const void* b,
                        int storage_b, double* out_dev, void* stream);
 

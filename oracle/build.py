@@ -2,8 +2,10 @@
 
 ``build_oracle()`` compiles the C restatement ``oracle/st3d_oracle.c`` into
 ``oracle/_build/libst3d_oracle.so``.  ``build_ref()`` compiles the reference's
-own host path from its sources, where they are present, with
-``oracle/Makefile.ref`` into ``oracle/_ref/``.
+own host path from its sources with ``oracle/Makefile.ref`` into
+``oracle/_ref/``; the directory holding the reference's sources is named by
+the environment variable ``ST3D_REFERENCE_DIR`` (no default: without it, or
+where the sources are absent, nothing is built).
 """
 import os
 import subprocess
@@ -12,7 +14,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 ORACLE_SO = os.path.join(HERE, "_build", "libst3d_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("ST3D_REFERENCE_DIR", "/root/reference")
+
+
+def ref_source_dir():
+    """The reference's source directory (ST3D_REFERENCE_DIR), or None."""
+    d = os.environ.get("ST3D_REFERENCE_DIR")
+    return d if d and os.path.isfile(os.path.join(d, "iterators.cpp")) else None
 
 
 def build_oracle(force=False):
@@ -28,11 +35,12 @@ def build_oracle(force=False):
 
 
 def build_ref():
-    """Compile oracle/_ref from the reference sources; False if they are absent."""
-    if not os.path.isfile(os.path.join(REF_SRC, "iterators.cpp")):
+    """Compile oracle/_ref from the reference sources; False if they are not given."""
+    src = ref_source_dir()
+    if src is None:
         return False
     subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"),
-                    "REFDIR=" + REF_SRC, "OUT=" + REF_DIR, "-j8"],
+                    "REFDIR=" + src, "OUT=" + REF_DIR, "-j8"],
                    check=True, cwd=REPO)
     return True
 

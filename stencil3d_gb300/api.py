@@ -50,7 +50,7 @@ class Opts(C.Structure):
                 ("src_f", C.c_double), ("src_t0", C.c_double), ("dt", C.c_double),
                 ("temporal_block", C.c_int32), ("tile_j", C.c_int32), ("tile_k", C.c_int32),
                 ("ichunk", C.c_int32), ("stages", C.c_int32), ("host_path", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("device", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Info(C.Structure):
@@ -62,7 +62,7 @@ class Info(C.Structure):
                 ("bytes_per_point", C.c_double), ("flops_per_point", C.c_double),
                 ("tile_j", C.c_int32), ("tile_k", C.c_int32), ("ichunk", C.c_int32),
                 ("temporal_block", C.c_int32), ("host_path", C.c_int32), ("tb_tile_j", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("device", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Metrics(C.Structure):
@@ -110,6 +110,7 @@ def lib():
             "st3d_iterate": ([vp, C.c_uint32], i),
             "st3d_iterate_host": ([vp, vp, vp, vp, C.c_uint32], i),
             "st3d_synchronize": ([vp], i),
+            "st3d_inject_device_status": ([vp, C.c_uint32], i),
             "st3d_fill": ([vp, i, i, C.c_uint64, C.c_double, C.c_double], i),
             "st3d_check": ([vp, C.c_double, C.c_double, C.POINTER(C.c_uint64)], i),
             "st3d_norms": ([vp, i, vp, i, C.POINTER(C.c_double)], i),
@@ -315,6 +316,11 @@ class Stencil:
 
     def synchronize(self):
         _ck(lib().st3d_synchronize(self._h))
+
+    def inject_device_status(self, code):
+        """Diagnostics: set the device status word as a timed-out device wait
+        does (st3d_synchronize then reports ST3D_ERR_TIMEOUT once)."""
+        _ck(lib().st3d_inject_device_status(self._h, int(code)))
 
     def fill(self, field, kind, seed=0, a=0.0, b=0.0):
         _ck(lib().st3d_fill(self._h, field, kind, seed, a, b))

@@ -2,7 +2,8 @@
 
 Compiles the CUDA sources under ``csrc/`` for sm_103a (GB300) into
 ``_build/libst3d.so`` and the hstencil3d-compatible command line driver
-``_build/gstencil3d`` (host C++ over the C ABI).  Translation units compile in
+``_build/gstencil3d`` (host C++ over the C ABI; ``_build/gstencil3d_f64`` is
+the same driver built with USE_DOUBLE, the reference's double build).  Translation units compile in
 parallel; nothing here needs a GPU.
 """
 import concurrent.futures as cf
@@ -18,6 +19,7 @@ HOST = os.path.join(HERE, "host")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libst3d.so")
 CLI = os.path.join(OUT, "gstencil3d")
+CLI_F64 = os.path.join(OUT, "gstencil3d_f64")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -80,10 +82,11 @@ def build(verbose=False, force=False, ptxas_info=False):
     host_src = [os.path.join(HOST, f) for f in ("gstencil3d.cpp", "st3d_compat.cpp")]
     if all(os.path.exists(p) for p in host_src):
         host_hdr = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith((".h", ".hpp"))]
-        if force or _newer(CLI, host_src + host_hdr + hdrs + [LIB]):
-            _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp",
-                  "-I", os.path.join(REPO, "include"), "-I", HOST, "-o", CLI] + host_src +
-                 ["-L", OUT, "-lst3d", "-Wl,-rpath,$ORIGIN"], verbose)
+        for exe, defs in ((CLI, []), (CLI_F64, ["-DUSE_DOUBLE"])):
+            if force or _newer(exe, host_src + host_hdr + hdrs + [LIB]):
+                _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp"] + defs +
+                     ["-I", os.path.join(REPO, "include"), "-I", HOST, "-o", exe] + host_src +
+                     ["-L", OUT, "-lst3d", "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
 

@@ -145,21 +145,14 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
   if (elem_bytes(o->storage) == 0) return fail(ST3D_ERR_INVALID, "unknown storage %d", o->storage);
   if (o->kernel < ST3D_KERNEL_AUTO || o->kernel > ST3D_KERNEL_TMA)
     return fail(ST3D_ERR_INVALID, "unknown kernel %d", o->kernel);
-  if (g->xs < 1 || g->ys < 1 || g->zs < 1)
-    return fail(ST3D_ERR_INVALID, "grid sizes must be >= 1 (got %u x %u x %u)", g->xs, g->ys, g->zs);
-  if ((uint64_t)g->xs * g->ys * g->zs > (1ull << 36))
-    return fail(ST3D_ERR_INVALID, "grid of %llu points is beyond the library limit 2^36",
-                (unsigned long long)g->xs * g->ys * g->zs);
-  if (g->zs > (1u << 24) || g->ys > (1u << 24) || g->xs > (1u << 24))
-    return fail(ST3D_ERR_INVALID, "grid axis beyond 2^24 points");
+  const int grc = st3d::validate_grid_limits(g);
+  if (grc != ST3D_OK) return grc;
   // The stencil reads u up to R points beyond the interior on every axis
   // (stencil_*.h neighbour loads); the 2-point stencil only reads k+1.
   const uint32_t rx = o->points == 2 ? 0 : R, ry = rx, rz = R;
   if (g->xh < rx || g->yh < ry || g->zh < rz)
     return fail(ST3D_ERR_INVALID, "halo (%u,%u,%u) is narrower than the %d-point stencil needs (%u,%u,%u)",
                 g->xh, g->yh, g->zh, o->points, rx, ry, rz);
-  if (g->xh > 64 || g->yh > 64 || g->zh > 4096)
-    return fail(ST3D_ERR_INVALID, "halo (%u,%u,%u) too wide", g->xh, g->yh, g->zh);
   if (o->mode == ST3D_MODE_WAVE && o->points == 2)
     return fail(ST3D_ERR_UNSUPPORTED, "the 2-point stencil has no wave form (it is not a Laplacian)");
   const bool s16 = o->storage == ST3D_F16 || o->storage == ST3D_BF16 || o->storage == ST3D_F16_HILO ||
@@ -192,6 +185,9 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_UNSUPPORTED,
                 "temporal blocking depth %d is too deep for the %d-point stencil (at most %d)",
                 o->temporal_block, o->points, o->points == 7 ? 4 : 2);
+  if (o->device < -1)
+    return fail(ST3D_ERR_INVALID, "device %d: a CUDA device ordinal, or -1 for the current device",
+                o->device);
   if (o->mode == ST3D_MODE_WAVE && o->src_i >= 0 &&
       ((uint32_t)o->src_i >= g->xs || o->src_j < 0 || (uint32_t)o->src_j >= g->ys ||
        o->src_k < 0 || (uint32_t)o->src_k >= g->zs))
@@ -799,6 +795,23 @@ int check_device_status(st3d_ctx* c) {
 }  // namespace
 
 namespace st3d {
+// Limits of a grid that every entry point taking one applies: each axis
+// 1 .. 2^24 points, at most 2^36 interior points, halos at most 64/64/4096.
+int validate_grid_limits(const st3d_grid_desc* g) {
+  if (!g) return fail(ST3D_ERR_INVALID, "null grid");
+  if (g->xs < 1 || g->ys < 1 || g->zs < 1)
+    return fail(ST3D_ERR_INVALID, "grid sizes must be >= 1 (got %u x %u x %u)", g->xs, g->ys, g->zs);
+  if (g->zs > (1u << 24) || g->ys > (1u << 24) || g->xs > (1u << 24))
+    return fail(ST3D_ERR_INVALID, "grid axis beyond 2^24 points (got %u x %u x %u)", g->xs, g->ys,
+                g->zs);
+  if ((uint64_t)g->xs * g->ys * g->zs > (1ull << 36))
+    return fail(ST3D_ERR_INVALID, "grid of %llu points is beyond the library limit 2^36",
+                (unsigned long long)g->xs * g->ys * g->zs);
+  if (g->xh > 64 || g->yh > 64 || g->zh > 4096)
+    return fail(ST3D_ERR_INVALID, "halo (%u,%u,%u) too wide", g->xh, g->yh, g->zh);
+  return ST3D_OK;
+}
+
 // FP32 tiled tensor map over one field buffer (encode_map above), for the
 // batch kernel's own tile shapes.
 int encode_f32_box(CUtensorMap* m, void* base, const Layout& L, uint32_t box_k, uint32_t box_j,
@@ -856,6 +869,7 @@ int st3d_default_opts(int points, int mode, int storage, st3d_opts* o) {
   o->storage = storage;
   o->kernel = ST3D_KERNEL_AUTO;
   o->temporal_block = 1;
+  o->device = -1;  // the calling thread's current device
   o->src_i = -2;  // grid centre, resolved at st3d_create
   o->src_f = 15.0;
   o->src_t0 = 1.0 / 15.0;
@@ -956,6 +970,7 @@ int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info
   info->tile_k = tma ? kTmaTK : 0;
   info->ichunk = opts->ichunk > 0 ? opts->ichunk : (tma ? 128 : 64);
   info->temporal_block = opts->temporal_block > 0 ? opts->temporal_block : 1;
+  info->device = opts->device;
   return ST3D_OK;
 }
 
@@ -973,6 +988,16 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
   *out = nullptr;
   int rc = validate(grid, opts);
   if (rc != ST3D_OK) return rc;
+  if (opts->device >= 0) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      return fail(ST3D_ERR_NODEVICE, "no CUDA device visible");
+    }
+    if (opts->device >= ndev)
+      return fail(ST3D_ERR_INVALID, "device %d out of range (%d devices visible)", opts->device, ndev);
+  }
+  DeviceScope scope(opts->device);
   int sm = 0, ccM = 0, ccm = 0;
   size_t total = 0;
   rc = st3d_device_info(&sm, &ccM, &ccm, &total);
@@ -1124,6 +1149,7 @@ extern "C" {
 
 int st3d_destroy(st3d_ctx* c) {
   if (!c) return ST3D_OK;
+  DeviceScope scope(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (int f = 0; f < 5; ++f)
     if (c->fld[f]) cudaFree(c->fld[f]);
@@ -1165,6 +1191,7 @@ int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
   info->temporal_block = c->opts.temporal_block;
   info->host_path = c->host_path;
   info->tb_tile_j = c->tb ? c->tb->rows : 0;
+  info->device = c->device;
   return ST3D_OK;
 }
 
@@ -1184,6 +1211,7 @@ int st3d_transfer(st3d_ctx* dst, st3d_ctx* src) {
   if (host_elem_bytes(dst->opts.storage) != host_elem_bytes(src->opts.storage))
     return fail(ST3D_ERR_UNSUPPORTED, "transfer between FP64 and FP32-valued storages");
   if (dst->device != src->device) return fail(ST3D_ERR_UNSUPPORTED, "transfer across devices");
+  DeviceScope scope(src->device);
   if (!(src->has_u && src->has_v)) return fail(ST3D_ERR_STATE, "the source context holds no u and v");
   const size_t bytes = host_array_bytes(src);
   void* buf = nullptr;
@@ -1218,6 +1246,7 @@ int st3d_get_stream(const st3d_ctx* c, void** s) {
 
 int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  DeviceScope scope(c->device);
   int rc;
   if (c->delta) {
     c->step = 0;
@@ -1282,6 +1311,7 @@ int st3d_upload(st3d_ctx* c, const void* v, const void* s, const void* u) {
 
 int st3d_download(st3d_ctx* c, void* v, void* u) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  DeviceScope scope(c->device);
   int rc;
   if (c->delta) {
     if (v && (rc = delta_download(c, v, true)) != ST3D_OK) return rc;
@@ -1303,6 +1333,7 @@ int st3d_download(st3d_ctx* c, void* v, void* u) {
 
 int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  DeviceScope scope(c->device);
   if (!(c->has_u && c->has_v && c->has_s))
     return fail(ST3D_ERR_STATE, "upload or fill u, v and s before iterating");
   const bool wave = c->opts.mode == ST3D_MODE_WAVE;
@@ -1402,13 +1433,24 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
 
 int st3d_synchronize(st3d_ctx* c) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  DeviceScope scope(c->device);
   ST3D_CUDA(cudaStreamSynchronize(c->stream));
-  if (c->kernel == ST3D_KERNEL_TMA || c->tb) return check_device_status(c);
+  return check_device_status(c);
+}
+
+int st3d_inject_device_status(st3d_ctx* c, uint32_t code) {
+  if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  DeviceScope scope(c->device);
+  ST3D_CUDA(cudaMemsetAsync(c->dev_status, 0, sizeof(uint32_t), c->stream));
+  if (code != 0)
+    ST3D_CUDA(cudaMemcpyAsync(c->dev_status, &code, sizeof code, cudaMemcpyHostToDevice, c->stream));
+  ST3D_CUDA(cudaStreamSynchronize(c->stream));
   return ST3D_OK;
 }
 
 int st3d_iterate_host(st3d_ctx* c, void* v, const void* s, void* u, uint32_t iterations) {
   if (!c || !v || !s || !u) return fail(ST3D_ERR_INVALID, "null argument");
+  DeviceScope scope(c->device);
   int rc = st3d_upload(c, v, s, u);
   if (rc == ST3D_OK) rc = st3d_iterate(c, iterations);
   if (rc == ST3D_OK)
@@ -1419,6 +1461,7 @@ int st3d_iterate_host(st3d_ctx* c, void* v, const void* s, void* u, uint32_t ite
 
 int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double b) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  DeviceScope scope(c->device);
   if (field < ST3D_FIELD_U || field > ST3D_FIELD_S) return fail(ST3D_ERR_INVALID, "bad field %d", field);
   if (kind < ST3D_FILL_CONST || kind > ST3D_FILL_BLOBS) return fail(ST3D_ERR_INVALID, "bad fill kind %d", kind);
   void* dst = field == ST3D_FIELD_U ? u_ptr(c) : field == ST3D_FIELD_V ? v_ptr(c) : c->fld[2];
@@ -1502,6 +1545,7 @@ int st3d_fill(st3d_ctx* c, int field, int kind, uint64_t seed, double a, double 
 
 int st3d_check(st3d_ctx* c, double expected, double tol, uint64_t* errors) {
   if (!c || !errors) return fail(ST3D_ERR_INVALID, "null argument");
+  DeviceScope scope(c->device);
   ST3D_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned long long), c->stream));
   cudaError_t e = launch_check(c->G, field_ref(c, ST3D_FIELD_V), expected, tol, c->counter, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "check kernel launch");
@@ -1514,6 +1558,8 @@ int st3d_check(st3d_ctx* c, double expected, double tol, uint64_t* errors) {
 
 int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]) {
   if (!a || !out) return fail(ST3D_ERR_INVALID, "null argument");
+  if (b && b->device != a->device) return fail(ST3D_ERR_UNSUPPORTED, "norms across devices");
+  DeviceScope scope(a->device);
   if (b && (b->grid.xs != a->grid.xs || b->grid.ys != a->grid.ys || b->grid.zs != a->grid.zs))
     return fail(ST3D_ERR_INVALID, "norms need equal interior sizes");
   if (fa < 0 || fa > 2 || (b && (fb < 0 || fb > 2))) return fail(ST3D_ERR_INVALID, "bad field");
@@ -1539,6 +1585,7 @@ int st3d_norms(st3d_ctx* a, int fa, st3d_ctx* b, int fb, double out[4]) {
 
 int st3d_timer_start(st3d_ctx* c) {
   if (!c) return fail(ST3D_ERR_INVALID, "null context");
+  DeviceScope scope(c->device);
   ST3D_CUDA(cudaEventRecord(c->ev0, c->stream));
   c->timer_step0 = c->lvl;
   return ST3D_OK;
@@ -1546,6 +1593,7 @@ int st3d_timer_start(st3d_ctx* c) {
 
 int st3d_timer_stop(st3d_ctx* c, float* ms) {
   if (!c || !ms) return fail(ST3D_ERR_INVALID, "null argument");
+  DeviceScope scope(c->device);
   ST3D_CUDA(cudaEventRecord(c->ev1, c->stream));
   ST3D_CUDA(cudaEventSynchronize(c->ev1));
   ST3D_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev1));
@@ -1556,6 +1604,7 @@ int st3d_timer_stop(st3d_ctx* c, float* ms) {
 
 int st3d_metrics_get(st3d_ctx* c, st3d_ctx* ref, st3d_metrics* m) {
   if (!c || !m) return fail(ST3D_ERR_INVALID, "null argument");
+  DeviceScope scope(c->device);
   memset(m, 0, sizeof *m);
   m->steps = c->step;
   m->timed_steps = c->timed_steps;

@@ -344,6 +344,7 @@ struct st3d_batch {
   uint64_t launches = 0;
   uint64_t points = 0;
   std::map<uint32_t, cudaGraphExec_t> graphs;  // by step count
+  int device = -1;  // CUDA device ordinal of every grid (opts.device), -1: current
 };
 
 namespace {
@@ -454,13 +455,26 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
     if (o.mode != ST3D_MODE_WAVE || o.storage != ST3D_F32 || o.points == 2)
       return set_error(ST3D_ERR_UNSUPPORTED,
                        "batch grid %u: the batching form runs the FP32 wave update of 7/13/25 points", gi);
+    if (o.device != opts[0].device)
+      return set_error(ST3D_ERR_INVALID, "batch grid %u: every grid of a batch runs on one device", gi);
   }
+  if (opts[0].device < -1) return bfail(ST3D_ERR_INVALID, "bad device ordinal");
+  if (opts[0].device >= 0) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      return bfail(ST3D_ERR_NODEVICE, "no CUDA device visible");
+    }
+    if (opts[0].device >= ndev) return bfail(ST3D_ERR_INVALID, "device ordinal out of range");
+  }
+  DeviceScope scope(opts[0].device);
   st3d_batch* b = new (std::nothrow) st3d_batch();
   if (!b) return bfail(ST3D_ERR_NOMEM, "host allocation failed");
   auto cleanup = [b](int rc) {
     st3d_batch_destroy(b);
     return rc;
   };
+  cudaGetDevice(&b->device);
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->amps_copied, cudaEventDisableTiming) != cudaSuccess) {
@@ -560,6 +574,7 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
 
 int st3d_batch_destroy(st3d_batch* b) {
   if (!b) return ST3D_OK;
+  DeviceScope scope(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   destroy_graphs(b);
   for (st3d_ctx* c : b->ctx) st3d_destroy(c);
@@ -598,6 +613,7 @@ int st3d_batch_get_info(const st3d_batch* b, st3d_batch_info* info) {
 
 int st3d_batch_iterate(st3d_batch* b, uint32_t steps, int schedule) {
   if (!b) return bfail(ST3D_ERR_INVALID, "null batch");
+  DeviceScope scope(b->device);
   if (steps == 0) return ST3D_OK;
   for (st3d_ctx* c : b->ctx)
     if (!(c->has_u && c->has_v && c->has_s))
@@ -640,6 +656,7 @@ int st3d_batch_iterate(st3d_batch* b, uint32_t steps, int schedule) {
 
 int st3d_batch_synchronize(st3d_batch* b) {
   if (!b) return bfail(ST3D_ERR_INVALID, "null batch");
+  DeviceScope scope(b->device);
   B_CUDA(cudaStreamSynchronize(b->stream));
   uint32_t st = 0;
   B_CUDA(cudaMemcpy(&st, b->d_status, sizeof st, cudaMemcpyDeviceToHost));
@@ -656,12 +673,14 @@ int st3d_batch_synchronize(st3d_batch* b) {
 
 int st3d_batch_timer_start(st3d_batch* b) {
   if (!b) return bfail(ST3D_ERR_INVALID, "null batch");
+  DeviceScope scope(b->device);
   B_CUDA(cudaEventRecord(b->ev0, b->stream));
   return ST3D_OK;
 }
 
 int st3d_batch_timer_stop(st3d_batch* b, float* ms) {
   if (!b || !ms) return bfail(ST3D_ERR_INVALID, "null argument");
+  DeviceScope scope(b->device);
   B_CUDA(cudaEventRecord(b->ev1, b->stream));
   B_CUDA(cudaEventSynchronize(b->ev1));
   B_CUDA(cudaEventElapsedTime(ms, b->ev0, b->ev1));

@@ -71,6 +71,37 @@ struct Coefs {
 template <typename C>
 Coefs<C> make_coefs(const st3d_opts& o);
 
+// Makes `dev` the calling thread's current CUDA device for the scope of one
+// entry point and restores the previous device on exit, so that a context
+// created on device N runs there whatever device the caller has current.
+// dev < 0: leave the current device as it is.
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(int dev) {
+    if (dev < 0) return;
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+      return;
+    }
+    if (prev == dev) {
+      prev = -1;
+    } else if (cudaSetDevice(dev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
+// The grid limits every entry point applies (st3d_api.cu): axes 1 .. 2^24,
+// at most 2^36 points, halos at most 64/64/4096; ST3D_OK or the status.
+int validate_grid_limits(const st3d_grid_desc* g);
+
 // Geometry passed to kernels by value.
 struct Geom {
   int xs, ys, zs;

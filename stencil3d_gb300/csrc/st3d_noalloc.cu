@@ -22,7 +22,14 @@
 //     caller;
 //   - the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (the array's name in host code is only a host-side
-//     stand-in); make that first call before any stream capture.
+//     stand-in); make that first call before any stream capture.  The address
+//     is kept per device together with the identity of the CUDA context it
+//     was looked up in: after a cudaDeviceReset (or any teardown and
+//     re-creation of the device's context) the next call finds a new context
+//     and looks the address up again, so that first call after a reset must
+//     also come before any stream capture.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "st3d_internal.h"
@@ -37,7 +44,9 @@ constexpr int kNoAllocThreads = 256;
 // Per-plane partials: [4*i + 0..3] = sum (a-b)^2, sum b^2, max|a-b|, max|b|.
 static __device__ __align__(256) double g_plane_partials[4 * kNoAllocMaxPlanes];
 
+// per device: the partials' address and the ID of the context it belongs to
 double* g_partials_dev[kNoAllocMaxDevices] = {nullptr};
+unsigned long long g_partials_ctx[kNoAllocMaxDevices] = {0};
 std::mutex g_setup_mutex;
 
 struct RefLayout {
@@ -112,8 +121,40 @@ __global__ void __launch_bounds__(kNoAllocThreads)
   if (threadIdx.x < 4) out[threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// Unique ID of the calling thread's current CUDA context (0 if none is
+// current yet, or if the driver does not answer).  The driver calls are taken
+// through the runtime's entry-point query, so the library keeps no link-time
+// dependence on the driver library.
+typedef CUresult (*PFN_ctx_get_current)(CUcontext*);
+typedef CUresult (*PFN_ctx_get_id)(CUcontext, unsigned long long*);
+
+unsigned long long current_context_id() {
+  static PFN_ctx_get_current get_current = nullptr;
+  static PFN_ctx_get_id get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_ctx_get_current>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_ctx_get_id>(f);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id) return 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
 // Device address of the partials array on the current device, looked up once
-// per device; nullptr (with `err` set) if the lookup fails.
+// per device and context; nullptr (with `err` set) if the lookup fails.
 double* noalloc_partials(cudaError_t* err) {
   int dev = 0;
   *err = cudaGetDevice(&dev);
@@ -123,11 +164,17 @@ double* noalloc_partials(cudaError_t* err) {
     return nullptr;
   }
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_partials_dev[dev]) {
+  const unsigned long long id = current_context_id();
+  if (!g_partials_dev[dev] || id == 0 || id != g_partials_ctx[dev]) {
     double* p = nullptr;
     *err = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_plane_partials);
-    if (*err != cudaSuccess) return nullptr;
+    if (*err != cudaSuccess) {
+      g_partials_dev[dev] = nullptr;
+      return nullptr;
+    }
     g_partials_dev[dev] = p;
+    // the lookup made the device's context current if it was not yet
+    g_partials_ctx[dev] = id != 0 ? id : current_context_id();
   }
   return g_partials_dev[dev];
 }
@@ -158,8 +205,10 @@ extern "C" int st3d_norms_noalloc(const st3d_grid_desc* grid, const void* a, int
   if ((storage_a != ST3D_F32 && storage_a != ST3D_F64) ||
       (b && storage_b != ST3D_F32 && storage_b != ST3D_F64))
     return set_error(ST3D_ERR_INVALID, "fields must be F32 or F64");
-  if (grid->xs < 1 || grid->ys < 1 || grid->zs < 1)
-    return set_error(ST3D_ERR_INVALID, "grid sizes must be >= 1");
+  // the limits of every other entry point (axes, point count, halos), then
+  // this entry point's own plane limit
+  const int grc = validate_grid_limits(grid);
+  if (grc != ST3D_OK) return grc;
   if (grid->xs > (uint32_t)kNoAllocMaxPlanes)
     return set_error(ST3D_ERR_INVALID,
                      "st3d_norms_noalloc handles at most %d planes along i (got %u); "

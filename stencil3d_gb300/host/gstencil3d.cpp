@@ -4,8 +4,9 @@
 // reference driver (main.cpp:94-332): the time loop runs on the GPU through
 // the C ABI, every other step stays on the host.  The stencil size, CPU
 // traversal (PAR2D/HILBERT/...) and `real` are compile-time choices in the
-// reference (config.h:19-65); here the stencil is a run-time flag and the
-// traversal flags are accepted and ignored.
+// reference (config.h:19-65, 96-100); here the stencil is a run-time flag,
+// the traversal flags are accepted and ignored, and `real` follows
+// USE_DOUBLE as in the reference (the double build runs the FP64 storage).
 //
 // Added flags: --stencil N (2, 7, 13, 25; default 7 as config.h:38),
 // --wave (the leapfrog form, README.md:11-20, with --vel/--dt/--dx),
@@ -63,7 +64,7 @@ int main(int argc, char** argv) {
   real sbm = 12;
   const char* kernel = "auto";
   const char* variant = "ref";
-  const char* storage = "f32";
+  const char* storage = sizeof(real) == sizeof(double) ? "f64" : "f32";
   unsigned tblock = 1;
   gb300_options gopt;
 
@@ -123,8 +124,15 @@ int main(int argc, char** argv) {
     return 2;
   }
   if (points == 13 && strcmp(variant, "vec16") == 0 && !wave) gopt.K = 6.25;
-  // host arrays are float (`real`): FP32 or one of the 16-bit device storages
-  if (strcmp(storage, "f32") == 0) gopt.storage = ST3D_F32;
+  // host arrays are `real`: double in the USE_DOUBLE build (FP64 storage),
+  // else float (FP32 or one of the 16-bit device storages)
+  if (sizeof(real) == sizeof(double)) {
+    if (strcmp(storage, "f64") != 0) {
+      fprintf(stderr, "--storage %s needs the float build (this one has USE_DOUBLE)\n", storage);
+      return 2;
+    }
+    gopt.storage = ST3D_F64;
+  } else if (strcmp(storage, "f32") == 0) gopt.storage = ST3D_F32;
   else if (strcmp(storage, "f16") == 0) gopt.storage = ST3D_F16;
   else if (strcmp(storage, "bf16") == 0) gopt.storage = ST3D_BF16;
   else if (strcmp(storage, "f16_hilo") == 0) gopt.storage = ST3D_F16_HILO;
@@ -133,7 +141,7 @@ int main(int argc, char** argv) {
     fprintf(stderr, "--storage must be f32, f16, bf16, f16_hilo or f16_hl\n");
     return 2;
   }
-  if (gopt.storage != ST3D_F32 && !wave) {
+  if (gopt.storage != ST3D_F32 && gopt.storage != ST3D_F64 && !wave) {
     fprintf(stderr, "--storage %s needs --wave\n", storage);
     return 2;
   }
@@ -179,7 +187,7 @@ int main(int argc, char** argv) {
   double t0 = seconds();
   init_arrays(ov, os, ou, asize / sizeof(real));
   // the 16-bit storages and fused steps hold a zero (Dirichlet) boundary
-  if (wave && (gopt.storage != ST3D_F32 || tblock > 1)) {
+  if (wave && ((gopt.storage != ST3D_F32 && gopt.storage != ST3D_F64) || tblock > 1)) {
     zero_halo(v, grid);
     zero_halo(s, grid);
     zero_halo(u, grid);

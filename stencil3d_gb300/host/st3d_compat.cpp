@@ -25,6 +25,12 @@ st3d_ctx* context_for(const s_grid& g) {
   const unsigned key[6] = {g.xsize, g.ysize, g.zsize, g.xhalo, g.yhalo, g.zhalo};
   if (g_ctx && memcmp(key, g_key, sizeof key) == 0) return g_ctx;
   gb300_release();
+  // the host arrays hold `real`: double only for the FP64 storage
+  if ((g_opts.storage == ST3D_F64) != (sizeof(real) == sizeof(double))) {
+    fprintf(stderr, "error: storage %d does not match the host arrays' %zu-byte real\n",
+            g_opts.storage, sizeof(real));
+    exit(3);
+  }
   st3d_grid_desc d = {g.xsize, g.ysize, g.zsize, g.xhalo, g.yhalo, g.zhalo};
   st3d_opts o;
   int rc = st3d_default_opts(g_opts.points, g_opts.mode, g_opts.storage, &o);

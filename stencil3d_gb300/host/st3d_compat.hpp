@@ -17,7 +17,13 @@
 
 #include "st3d.h"
 
+// config.h:96-100: `real` is double in the reference's USE_DOUBLE build
+// (then the library runs its FP64 storage) and float otherwise.
+#ifdef USE_DOUBLE
+typedef double real;
+#else
 typedef float real;
+#endif
 
 class s_grid {
  public:
@@ -43,7 +49,11 @@ class s_grid {
 struct gb300_options {
   int points = 7;                 // STENCIL_SIZE
   int mode = ST3D_MODE_REF;
-  int storage = ST3D_F32;         // float; USE_DOUBLE -> ST3D_F64
+#ifdef USE_DOUBLE
+  int storage = ST3D_F64;         // real = double: FP64 fields and arithmetic
+#else
+  int storage = ST3D_F32;         // real = float: FP32 or a 16-bit device storage
+#endif
   int kernel = ST3D_KERNEL_AUTO;
   double vel = 1500.0, dt = 1e-3, dx = 10.0;  // mode W physics
   // Mode R diagonal coefficient K; 0 keeps the stencil's default.  The

@@ -19,11 +19,21 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 GPU (run with -m gpu)")
 
 
+# Where the reference's sources sit on the machine that built this checkout
+# (absent on the GPU machine, where the golden fixtures pin the oracle instead).
+_REFERENCE_SOURCES = "/root/reference"
+if "ST3D_REFERENCE_DIR" not in os.environ and os.path.isfile(
+        os.path.join(_REFERENCE_SOURCES, "iterators.cpp")):
+    os.environ["ST3D_REFERENCE_DIR"] = _REFERENCE_SOURCES
+
+
 @pytest.fixture(scope="session", autouse=True)
 def _native_builds():
-    """Build libst3d.so and the oracle in-tree if they are missing or stale."""
+    """Build libst3d.so, the oracle and, where its sources are given, the
+    reference's own host path (oracle/_ref) in-tree if missing or stale."""
     from stencil3d_gb300 import build as pbuild
     from oracle import build as obuild
     pbuild.build()
     obuild.build_oracle()
+    obuild.build_ref()
     yield

@@ -40,10 +40,11 @@ def test_struct_layout_matches_header(tmp_path):
     src = tmp_path / "sz.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "st3d.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(st3d_grid_desc),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(st3d_grid_desc),"
         " sizeof(st3d_opts), sizeof(st3d_info), offsetof(st3d_opts, c0),"
         " offsetof(st3d_opts, src_f), offsetof(st3d_info, bytes_per_point),"
-        " sizeof(st3d_metrics)); return 0;}\n")
+        " sizeof(st3d_metrics), offsetof(st3d_opts, device), offsetof(st3d_info, device));"
+        " return 0;}\n")
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)],
                    check=True)
@@ -51,12 +52,12 @@ def test_struct_layout_matches_header(tmp_path):
                                            check=True).stdout.split()]
     assert vals == [C.sizeof(api.GridDesc), C.sizeof(api.Opts), C.sizeof(api.Info),
                     api.Opts.c0.offset, api.Opts.src_f.offset, api.Info.bytes_per_point.offset,
-                    C.sizeof(api.Metrics)]
+                    C.sizeof(api.Metrics), api.Opts.device.offset, api.Info.device.offset]
 
 
 def test_abi_version_and_strings():
     lib = S.lib()
-    assert lib.st3d_abi_version() == 1
+    assert lib.st3d_abi_version() == 2
     assert lib.st3d_status_string(0) == b"ok"
     assert b"out of order" in lib.st3d_status_string(6)
 
@@ -142,6 +143,21 @@ def test_plan_rejects_bad_requests(grid, opts, status):
     assert rc == status, S.last_error()
 
 
+def test_device_field_defaults_and_planning():
+    """opts.device: -1 (the current device) by default; st3d_plan reports
+    the requested ordinal and rejects one below -1."""
+    o = S.default_opts(25, "wave", "f32")
+    assert o.device == -1
+    g = S.Grid(16, 16, 16, 4, 4, 4)
+    assert S.plan(g, o).device == -1
+    o.device = 3
+    assert S.plan(g, o).device == 3
+    o.device = -2
+    info = api.Info()
+    assert S.lib().st3d_plan(C.byref(g.desc()), C.byref(o), C.byref(info)) == S.api.ERR_INVALID
+    assert "device" in S.last_error()
+
+
 def _gpu_visible():
     try:
         S.device_info()
@@ -159,6 +175,10 @@ def test_no_cpu_fallback_without_gpu():
     v = np.zeros(S.Grid(8, 8, 8, 4, 4, 4).shape, np.float32)
     with pytest.raises(S.St3dError):
         S.iterate_gb300(v, v.copy(), v.copy(), S.Grid(8, 8, 8, 4, 4, 4), points=7)
+    # an explicit device ordinal does not bring a CPU path either
+    with pytest.raises(S.St3dError) as e:
+        S.Stencil(S.Grid(16, 16, 16, 4, 4, 4), 25, device=0)
+    assert e.value.status == S.api.ERR_NODEVICE
 
 
 def test_grid_mirror_matches_reference_strides():
@@ -179,3 +199,20 @@ def test_host_check_and_init_arrays():
     assert np.all(u == 1) and np.all(s == 1) and np.all(v == 0)
     assert S.check(v, g, 0) == 0
     assert S.check(v, g, 1) == 6 * 5 * 4
+
+
+@pytest.mark.parametrize("desc,what", [
+    ((8, 1 << 25, 8, 4, 4, 4), "2^24"),          # ys beyond an axis limit (and INT_MAX as int)
+    ((8, 8, (1 << 31) + 5, 4, 4, 4), "2^24"),    # zs that an int cast would make negative
+    ((8, 8, 8, 65, 4, 4), "too wide"),           # halo beyond the library's limit
+    ((0, 8, 8, 4, 4, 4), ">= 1"),
+    ((4097, 8, 8, 4, 4, 4), "4096"),             # the allocation-free array's plane limit
+])
+def test_noalloc_norms_validate_the_grid_before_any_device_work(desc, what):
+    """st3d_norms_noalloc applies every entry point's grid limits before it
+    touches a GPU (no device is needed to see the refusal)."""
+    g = api.GridDesc(*desc)
+    rc = S.lib().st3d_norms_noalloc(C.byref(g), C.c_void_p(256), S.F32, None, S.F32,
+                                    C.c_void_p(256), None)
+    assert rc == S.api.ERR_INVALID
+    assert what in S.last_error()

@@ -51,3 +51,25 @@ def test_batch_workload_is_seeded_and_prefix_stable():
 def test_l2_note_uses_the_device_layout():
     info = SimpleNamespace(nk=1088, nj=1032, ni=1032)
     assert bench.l2_note(info) == "fields 13.9 GB >> 129 MB L2, no flush needed"
+
+
+def test_summary_is_short_and_last():
+    """The summary object closes the line and stays short enough to survive
+    in a kept tail of the output."""
+    form = {"value": 300.0, "speedup_vs_fp32": 0.75, "roofline": {"frac": 0.45},
+            "l2_err_vs_fp64": 6.6e-3}
+    tb = {"steps": 2000, "T1": {"value": 405.0}, "T2": {"value": 470.0}, "T4": {"value": 440.0}}
+    result = {"value": 398.3, "roofline": {"frac": 0.939}, "l2_err_fp32_vs_fp64": 3.4e-6,
+              "mode_r": {"value": 395.0, "roofline": {"frac": 0.93}},
+              "fp16": {"f16": form, "bf16": form, "f16_hl": form, "f16_hilo": form,
+                       "f16_guarded": {"value": 197.0, "l2_err_vs_fp64": 8.4e-4}},
+              "batch": {"sequential": {"value": 186.0}, "persistent": {"value": 357.0},
+                        "graph": {"value": 358.0}, "graph_vs_sequential": 1.92},
+              "temporal_blocking": {"wave7_1024": tb, "wave13_1040": tb, "wave25_1024": tb},
+              "configs": {"wave7_256": {"value": 300.0, "roofline": {"frac": 0.7}},
+                          "wave25_528": {"value": 380.0, "roofline": {"frac": 0.9}}},
+              "e2e": {"value": 126.5}}
+    sm = bench.summary_of(result)
+    text = json.dumps(sm)
+    assert len(text) < 1200, len(text)
+    assert sm["fp32"][0] == 398.3 and sm["f16"][1] == 0.75 and sm["tb_wave13_1040"]["steps"] == 2000

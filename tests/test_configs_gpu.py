@@ -1,12 +1,14 @@
 """Parity at the benchmark configurations' full sizes.
 
-  - 7 points, 256^3, 20 steps and 25 points, 528^3, 200 steps, mode R on
-    seeded u, v ~ U[-1, 1), s ~ U[0.5, 1.5): the library through the drop-in
-    call equals the oracle's fused flavour bit for bit, and the reference
-    order (the oracle's plain flavour, pinned to the compiled reference)
-    within 1e-5 relative L2;
-  - 13 points, 1040^3, leapfrog wave with 8 seeded Gaussian blobs: two steps
-    fused per pass equal plain steps bit for bit (device-side difference);
+  - 7 points, 256^3, 20 steps, 25 points, 528^3, 200 steps, and the
+    headline size, 25 points at 1024^3 for 20 steps (stencil_25_ref_1,
+    stencil_25.h:75-95), mode R on seeded u, v ~ U[-1, 1), s ~ U[0.5, 1.5):
+    the library through the drop-in call equals the oracle's fused flavour
+    bit for bit, and the reference order (the oracle's plain flavour, pinned
+    to the compiled reference) within 1e-5 relative L2;
+  - 13 points, 1040^3, leapfrog wave with 8 seeded Gaussian blobs, 21 steps:
+    plain steps equal the oracle's wave restatement bit for bit, and every
+    temporal-blocking depth served equals plain steps bit for bit;
   - the 64-grid batch (axes U{64..320}, orders {7, 13, 25}): the graph
     schedule equals the sequential one bit for bit on every grid;
   - 1264^3, the largest grid the reference's command line accepts, in FP32
@@ -21,8 +23,11 @@ from tests.helpers import mode_r_inputs, rel_l2
 
 pytestmark = pytest.mark.gpu
 
+# temporal-blocking depths the library serves for the 13-point stencil
+TB13 = (1, 2)
 
-@pytest.mark.parametrize("points,n,steps", [(7, 256, 20), (25, 528, 200)])
+
+@pytest.mark.parametrize("points,n,steps", [(7, 256, 20), (25, 528, 200), (25, 1024, 20)])
 def test_mode_r_full_size(points, n, steps):
     grid = (n, n, n, 4, 4, 16)
     v, s, u = mode_r_inputs(grid, 20251203 + points, "f32")
@@ -33,17 +38,18 @@ def test_mode_r_full_size(points, n, steps):
     vf = v.copy()
     O.iterate_ref(vf, s, u, grid, points, steps, fma=True)
     np.testing.assert_array_equal(O.interior(vg, grid), O.interior(vf, grid))
-    if n <= 256:
-        vp = v.copy()
-        O.iterate_ref(vp, s, u, grid, points, steps, fma=False)
-        assert rel_l2(O.interior(vg, grid), O.interior(vp, grid)) <= 1e-5
+    del vf
+    vp = v.copy()
+    O.iterate_ref(vp, s, u, grid, points, steps, fma=False)
+    assert rel_l2(O.interior(vg, grid), O.interior(vp, grid)) <= 1e-5
 
 
 def test_temporal_blocking_full_size():
     g = S.Grid(1040, 1040, 1040, 4, 4, 4)
+    grid = g.tuple
     ctx = []
     try:
-        for T in (1, 2):
+        for T in TB13:
             st = S.Stencil(g, 13, "wave", "f32", kernel="tma", temporal_block=T, dt=5e-4,
                            src=(520, 520, 520))
             ctx.append(st)
@@ -52,12 +58,24 @@ def test_temporal_blocking_full_size():
             st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
             st.iterate(21)
             st.synchronize()
-        for field in (S.FIELD_U, S.FIELD_V):
-            d2, b2, dm, bm = ctx[1].norms(field, ctx[0], field)
-            assert b2 > 0 and d2 == 0.0 and dm == 0.0
+        for other in ctx[1:]:
+            for field in (S.FIELD_U, S.FIELD_V):
+                d2, b2, dm, bm = other.norms(field, ctx[0], field)
+                assert b2 > 0 and d2 == 0.0 and dm == 0.0
+        # the plain steps against the oracle's restatement of the wave form
+        ug, vg = g.empty(), g.empty()
+        ctx[0].download(vg, ug)
     finally:
         for st in ctx:
             st.close()
+    u = O.fill_blobs(grid, 20251203, 8, 20.0)
+    v = u.copy()
+    s = np.zeros_like(u)
+    c0, c1, c2 = O.wave_constants(13, 1500.0, 5e-4, 10.0)
+    O.iterate_wave(u, v, s, grid, 13, 21, c0, c1, c2, src=(520, 520, 520),
+                   amps=O.ricker_amps(0, 21, 5e-4), fma=True)
+    np.testing.assert_array_equal(O.interior(ug, grid), O.interior(u, grid))
+    np.testing.assert_array_equal(O.interior(vg, grid), O.interior(v, grid))
 
 
 def test_batch_full_workload_graph_equals_sequential():

@@ -25,9 +25,13 @@ def _rank_main(rank, world, port, out):
     r.barrier()
     t = r.max(10.0 + rank)          # the slowest rank's time
     n = r.sum(len(shard(64, rank, world)))
+    # each replica's context names its own GPU (bench.py: device = LOCAL_RANK)
+    import stencil3d_gb300 as S
+    o = S.default_opts(25, "wave", "f32", device=r.local_rank)
+    dev = S.plan(S.Grid(16, 16, 16, 4, 4, 4), o).device
     r.barrier()
     r.close()
-    out.put((rank, t, n))
+    out.put((rank, t, n, dev))
 
 
 def test_two_gloo_ranks_agree_on_max_time_and_cover_all_grids():
@@ -42,8 +46,9 @@ def test_two_gloo_ranks_agree_on_max_time_and_cover_all_grids():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    assert [t for _, t, _ in res] == [11.0, 11.0]
-    assert [n for _, _, n in res] == [64.0, 64.0]
+    assert [t for _, t, _, _ in res] == [11.0, 11.0]
+    assert [n for _, _, n, _ in res] == [64.0, 64.0]
+    assert [d for _, _, _, d in res] == [0, 1]
 
 
 def test_shard_is_a_partition():

@@ -11,8 +11,10 @@ The test plays such a caller: it owns its device buffers (allocated here,
 outside the library), calls the entry point through the C ABI twice in a row
 on different grids -- the second with fewer planes, so partials left behind by
 the first call would show if they were read -- and checks each result
-against st3d_norms on contexts holding the same fields.  This file is named
-to be collected last.
+against st3d_norms on contexts holding the same fields: an FP32 field against
+an FP64 one and the reverse, on the legacy default stream and on a stream the
+test creates and synchronises itself (the use inside a host's time loop).
+This file is named to be collected last.
 """
 import ctypes as C
 import os
@@ -38,6 +40,9 @@ def _cudart():
     rt.cudaFree.argtypes = [C.c_void_p]
     rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
     rt.cudaDeviceSynchronize.argtypes = []
+    rt.cudaStreamCreate.argtypes = [C.POINTER(C.c_void_p)]
+    rt.cudaStreamSynchronize.argtypes = [C.c_void_p]
+    rt.cudaStreamDestroy.argtypes = [C.c_void_p]
     return rt
 
 
@@ -62,7 +67,9 @@ class DeviceBuffer:
 
 def _context_norms(grid, a, b):
     g = S.Grid(*grid)
-    with S.Stencil(g, 7, "ref", "f32") as ca, S.Stencil(g, 7, "ref", "f64") as cb:
+    sa = "f64" if a.dtype == np.float64 else "f32"
+    sb = "f64" if b.dtype == np.float64 else "f32"
+    with S.Stencil(g, 7, "ref", sa) as ca, S.Stencil(g, 7, "ref", sb) as cb:
         ca.upload(u=a)
         cb.upload(u=b)
         return ca.norms(S.FIELD_U, cb, S.FIELD_U), ca.norms(S.FIELD_U)
@@ -74,26 +81,49 @@ def _close(got, want):
     assert got[2] == want[2] and got[3] == want[3]
 
 
-def test_noalloc_norms_match_existing_entry_point_twice():
+@pytest.mark.parametrize("ta,tb", [(np.float32, np.float64), (np.float64, np.float32)],
+                         ids=["a_f32_b_f64", "a_f64_b_f32"])
+@pytest.mark.parametrize("own_stream", [False, True], ids=["default_stream", "own_stream"])
+def test_noalloc_norms_match_existing_entry_point_twice(ta, tb, own_stream):
     rt = _cudart()
     lib = S.lib()
+    code = {np.float32: S.F32, np.float64: S.F64}
+    stream = C.c_void_p()
+    if own_stream:
+        assert rt.cudaStreamCreate(C.byref(stream)) == 0
+    try:
+        _two_calls(rt, lib, ta, tb, code, stream)
+    finally:
+        if own_stream:
+            rt.cudaStreamDestroy(stream)
+
+
+def _two_calls(rt, lib, ta, tb, code, stream):
+    def wait():
+        if stream.value:
+            assert rt.cudaStreamSynchronize(stream) == 0
+        else:
+            assert rt.cudaDeviceSynchronize() == 0
+
     for grid, seed in (((40, 24, 70, 4, 4, 4), 1), ((17, 30, 33, 4, 5, 6), 2)):
-        a = O.fill_uniform(grid, seed, 0, -1.0, 1.0, np.float32)
-        b = O.fill_uniform(grid, seed, 1, -1.0, 1.0, np.float64)
+        a = O.fill_uniform(grid, seed, 0, -1.0, 1.0, ta)
+        b = O.fill_uniform(grid, seed, 1, -1.0, 1.0, tb)
         da, db, dout = DeviceBuffer(rt, a.nbytes), DeviceBuffer(rt, b.nbytes), DeviceBuffer(rt, 32)
         try:
             da.put(a)
             db.put(b)
             desc = api.GridDesc(*grid)
             out = np.zeros(4, np.float64)
-            rc = lib.st3d_norms_noalloc(C.byref(desc), da.ptr, S.F32, db.ptr, S.F64, dout.ptr, None)
+            rc = lib.st3d_norms_noalloc(C.byref(desc), da.ptr, code[ta], db.ptr, code[tb], dout.ptr,
+                                        stream)
             assert rc == 0, S.last_error()
-            assert rt.cudaDeviceSynchronize() == 0
+            wait()
             dout.get(out)
             energy = np.zeros(4, np.float64)
-            rc = lib.st3d_norms_noalloc(C.byref(desc), da.ptr, S.F32, None, S.F64, dout.ptr, None)
+            rc = lib.st3d_norms_noalloc(C.byref(desc), da.ptr, code[ta], None, code[tb], dout.ptr,
+                                        stream)
             assert rc == 0, S.last_error()
-            assert rt.cudaDeviceSynchronize() == 0
+            wait()
             dout.get(energy)
         finally:
             for d in (da, db, dout):
