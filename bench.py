@@ -57,7 +57,7 @@ WORKLOADS = {
     "wave13_512": (13, 512, 512, 512, 4, 5e-4, "blobs"),
 }
 # fused steps per pass served for each stencil order
-TB_DEPTHS = {7: (1, 2, 4), 13: (1, 2)}
+TB_DEPTHS = {7: (1, 2, 4), 13: (1, 2, 4), 25: (1, 2)}
 # timed steps of a temporal-blocking workload that has a stated run length:
 # the 13-point 1040^3 configuration runs 2000 steps at every depth
 TB_STEPS = {"wave13_1040": 2000}
@@ -96,7 +96,7 @@ def parse():
                    help="storage the guarded FP16 run moves to past half the tolerance")
     p.add_argument("--fp64-steps", type=int, default=5,
                    help="timed steps of the FP64 (USE_DOUBLE) run of the workload (0 to skip)")
-    p.add_argument("--temporal-workloads", default="wave7_1024,wave13_1040",
+    p.add_argument("--temporal-workloads", default="wave7_1024,wave13_1040,wave25_1024",
                    help="workloads timed with 1, 2 and 4 fused steps per pass ('' to skip)")
     p.add_argument("--temporal-steps", type=int, default=40,
                    help="timed steps of each temporal-blocking run without a stated run length "

@@ -176,15 +176,15 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_INVALID, "temporal blocking depth must be 1, 2 or 4 (got %d)",
                 o->temporal_block);
   if (o->temporal_block > 1 &&
-      (o->mode != ST3D_MODE_WAVE || o->storage != ST3D_F32 || (o->points != 7 && o->points != 13)))
+      (o->mode != ST3D_MODE_WAVE || o->storage != ST3D_F32 || o->points == 2))
     return fail(ST3D_ERR_UNSUPPORTED,
-                "temporal blocking fuses FP32 wave steps of the 7- and 13-point stencils");
+                "temporal blocking fuses FP32 wave steps of the 7-, 13- and 25-point stencils");
   // a level tile loses R columns per fused step at either edge; the tile
-  // keeps 4 columns of margin, so (T - 1) * R <= 4
-  if (o->temporal_block > 1 && (o->temporal_block - 1) * radius_of(o->points) > 4)
+  // keeps at most 8 columns of margin, so (T - 1) * R <= 8
+  if (o->temporal_block > 1 && (o->temporal_block - 1) * radius_of(o->points) > 8)
     return fail(ST3D_ERR_UNSUPPORTED,
                 "temporal blocking depth %d is too deep for the %d-point stencil (at most %d)",
-                o->temporal_block, o->points, o->points == 7 ? 4 : 2);
+                o->temporal_block, o->points, o->points == 25 ? 2 : 4);
   if (o->device < -1)
     return fail(ST3D_ERR_INVALID, "device %d: a CUDA device ordinal, or -1 for the current device",
                 o->device);
@@ -736,8 +736,8 @@ int delta_download(st3d_ctx* c, void* host, bool v) {
   return ST3D_OK;
 }
 
-// Temporally blocked plan: work units of (16 - 2(T-1)R) rows x 120 columns x
-// ichunk planes; the warm-up of a unit is 2*T*R planes.
+// Temporally blocked plan: work units of (tb_rows - 2(T-1)R) rows x (128 -
+// 2 tb_khalo) columns x ichunk planes; the warm-up of a unit is 2*T*R planes.
 int plan_tb(st3d_ctx* c, int sm_count) {
   TbPlan* p = new (std::nothrow) TbPlan();
   if (!p) return fail(ST3D_ERR_NOMEM, "host allocation failed");
@@ -758,7 +758,8 @@ int plan_tb(st3d_ctx* c, int sm_count) {
     return fail(ST3D_ERR_UNSUPPORTED, "the temporally blocked kernel cannot be resident");
   }
   p->ntj = (int)((c->L.ys + p->rows_out - 1) / p->rows_out);
-  p->ntk = (int)((c->L.zs + 119) / 120);
+  const int outc = 128 - 2 * tb_khalo(c->opts.points, T);
+  p->ntk = (int)((c->L.zs + outc - 1) / outc);
   const int ctas = sm_count * per_sm;
   p->ichunk = c->opts.ichunk > 0 ? c->opts.ichunk
                                  : tma_pick_ichunk((int)c->L.xs, p->ntj * p->ntk, ctas, 2 * T * R);

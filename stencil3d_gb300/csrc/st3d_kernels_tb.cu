@@ -15,17 +15,19 @@
 // entry of level t-2's queue above that.
 //
 // Tiles shrink by R per level: one consumer warp per row of a level-1 tile
-// of tb_rows(P, T) rows (rows j0 - (T-1)R ..; 26 for 7 points T=2, else 18),
-// 4 points per lane over 128 columns (k0 - 4 .. k0 + 123); the pass writes
-// the rows - 2(T-1)R middle rows and the 120 columns k0 .. k0 + 119.  Level 1
-// is exact over its whole tile (the level-0 TMA tile carries R rows and 4
-// columns of halo); a level above reads zeros beyond its tile's edge, so
-// level t is exact in all but (t-1)R rows and columns at either edge, which
-// bounds (T-1)R by the 4 spare columns: T = 2 or 4 for the 7-point stencil,
-// T = 2 for the 13-point one.  Levels outside the grid interior are the zero
-// halo (temporal blocking requires a zero boundary).  Output goes to two
-// other buffers (neighbouring tiles still read U^n and U^{n-1} while a tile
-// writes), so a context that blocks in time holds four field buffers.
+// of tb_rows(P, T) rows (rows j0 - (T-1)R ..; 26 for 7 points T=2, 15 for 13
+// points T=4 and 25 points T=2, else 18), 4 points per lane over 128 columns
+// (k0 - KH .. k0 + 127 - KH, KH = tb_khalo(P, T) = 4 or 8); the pass writes
+// the rows - 2(T-1)R middle rows and the 128 - 2 KH columns k0 .. k0 + 127 -
+// 2 KH.  Level 1 is exact over its whole tile (the level-0 TMA tile carries R
+// rows and 4 columns of halo); a level above reads zeros beyond its tile's
+// edge, so level t is exact in all but (t-1)R rows and columns at either
+// edge, which bounds (T-1)R by the KH margin columns: T = 2 or 4 for the 7-
+// and 13-point stencils, T = 2 for the 25-point one.  Levels outside the grid
+// interior are the zero halo (temporal blocking requires a zero boundary).
+// Output goes to two other buffers (neighbouring tiles still read U^n and
+// U^{n-1} while a tile writes), so a context that blocks in time holds four
+// field buffers.
 //
 // Arithmetic per level point is the single-step kernels' difference form in
 // the same order, so T fused steps give bit for bit the result of T plain
@@ -44,7 +46,6 @@ namespace st3d {
 namespace {
 
 constexpr int kCols = 128;      // level columns per tile (32 lanes x 4)
-constexpr int kOutCols = 120;   // columns written per tile
 constexpr int kW = kCols + 8;   // smem row width (4 floats of pad either side)
 
 struct TbArgs {
@@ -61,14 +62,23 @@ struct TbArgs {
 
 template <int P>
 struct RadTB {
-  static constexpr int value = (P == 13) ? 2 : 1;
+  static constexpr int value = (P == 25) ? 4 : (P == 13) ? 2 : 1;
 };
 
 // Pipeline stages: 13 points T=2 on 18 rows has room in shared memory for a
-// fourth (203 KB; 460 against 453 Gpts/s at 1024^3 with 3); the 7-point
-// tiles fill it with 3.
+// fourth (203 KB; 460 against 453 Gpts/s at 1024^3 with 3); the other tiles
+// fill it with 3.
 template <int P, int T>
-constexpr int tb_stages() { return P == 13 ? 4 : 3; }
+constexpr int tb_stages() { return (P == 13 && T == 2) ? 4 : 3; }
+
+// Slots per level ring.  Level t writes its plane at step n into slot
+// (n - tR) mod NL and level t+1 reads that slot at step n + R; the named
+// barrier that ends every step orders each read before the slot's next
+// write, which comes NL steps after the first, so NL = R + 1 suffices (a
+// slot is never read and written in the same step: R mod (R+1) != 0).  13
+// points T=4 takes R + 1 to fit 227 KB; the other depths keep R + 2.
+template <int P, int T>
+constexpr int tb_level_slots() { return RadTB<P>::value + ((P == 13 && T == 4) ? 1 : 2); }
 
 template <int P, int T, int NV>
 struct TbShape {
@@ -77,7 +87,9 @@ struct TbShape {
   static constexpr int QN = 2 * R + 1;
   static constexpr int NU = NV + R;                       // level-0 ring (TMA u tiles)
   static constexpr int NS = NV + (T - 1) * R;             // s ring (kept for the later levels)
-  static constexpr int NL = R + 2;                        // slots per level ring
+  static constexpr int NL = tb_level_slots<P, T>();       // slots per level ring
+  static constexpr int KH = tb_khalo(P, T);               // k margin columns either side
+  static constexpr int OUTC = kCols - 2 * KH;             // columns written per tile
   static constexpr int USLOT = (kW * (kRows + 2 * R) + 31) / 32 * 32;  // floats
   static constexpr int VSLOT = kCols * kRows;             // floats
   static constexpr int LSLOT = kW * kRows;                // floats
@@ -96,6 +108,8 @@ __global__ void __launch_bounds__((tb_rows(P, T) + 1) * 32, 1)
   constexpr int QN = S::QN;
   constexpr int kRows = S::kRows;
   constexpr int NP = npairs_of(P);
+  constexpr int KH = S::KH;
+  constexpr int OUTC = S::OUTC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float* ur = reinterpret_cast<float*>(smem_raw);
   float* vr = ur + S::NU * S::USLOT;
@@ -129,7 +143,7 @@ __global__ void __launch_bounds__((tb_rows(P, T) + 1) * 32, 1)
       const int rem = unit - ic * a.ntjk;
       const int jt = rem / a.ntk;
       const int kt = rem - jt * a.ntk;
-      const int k0 = kt * kOutCols;
+      const int k0 = kt * OUTC;
       const int jb = jt * a.rows_out - (T - 1) * R;  // first level-1 row
       const int ia = ic * a.ichunk;
       const int ib = min(ia + a.ichunk, g.xs);
@@ -145,10 +159,11 @@ __global__ void __launch_bounds__((tb_rows(P, T) + 1) * 32, 1)
         const int p = ia - T * R + n;  // level-0 plane arriving
         const int p1 = p - R;          // level-1 plane of this step
         mbar_arrive_expect_tx(&full[stage], (uint32_t)(kW * (kRows + 2 * R) * 4 + 2 * S::VSLOT * 4));
-        tma_load_3d(ur + (h % S::NU) * S::USLOT, &umap, &full[stage], g.pk + k0 - 8, g.pj + jb - R,
-                    g.pi + p);
-        tma_load_3d(vr + stage * S::VSLOT, &vmap, &full[stage], g.pk + k0 - 4, g.pj + jb, g.pi + p1);
-        tma_load_3d(sr + (h % S::NS) * S::VSLOT, &smap, &full[stage], g.pk + k0 - 4, g.pj + jb,
+        // level column c sits at k0 - KH + c, smem column 4 + c of a u row
+        tma_load_3d(ur + (h % S::NU) * S::USLOT, &umap, &full[stage], g.pk + k0 - KH - 4,
+                    g.pj + jb - R, g.pi + p);
+        tma_load_3d(vr + stage * S::VSLOT, &vmap, &full[stage], g.pk + k0 - KH, g.pj + jb, g.pi + p1);
+        tma_load_3d(sr + (h % S::NS) * S::VSLOT, &smap, &full[stage], g.pk + k0 - KH, g.pj + jb,
                     g.pi + p1);
       }
     }
@@ -169,16 +184,16 @@ __global__ void __launch_bounds__((tb_rows(P, T) + 1) * 32, 1)
     const int rem = unit - ic * a.ntjk;
     const int jt = rem / a.ntk;
     const int kt = rem - jt * a.ntk;
-    const int k0 = kt * kOutCols;
+    const int k0 = kt * OUTC;
     const int jb = jt * a.rows_out - (T - 1) * R;
     const int j = jb + r;
-    const int kc = k0 - 4 + 4 * lane;  // first column of this lane
+    const int kc = k0 - KH + 4 * lane;  // first column of this lane
     const int ia = ic * a.ichunk;
     const int ib = min(ia + a.ichunk, g.xs);
     const int nsteps = (ib - ia) + 2 * T * R;
     const bool row_in = j >= 0 && j < g.ys;
     const bool out_row = r >= (T - 1) * R && r < kRows - (T - 1) * R && row_in;
-    const bool out_col = lane >= 1 && lane <= kOutCols / 4 && kc < g.zs;
+    const bool out_col = lane >= KH / 4 && lane < 32 - KH / 4 && kc < g.zs;
     // interior columns of this lane, and the source's column in it (or -1)
     bool colv[4];
 #pragma unroll
@@ -336,6 +351,8 @@ cudaError_t dispatch_tb(int points, int T, const TbPlan& pl, const TbArgs& a, co
   if (points == 7 && T == 2) return launch_pt<7, 2>(pl, a, u, v, s, stream, occ);
   if (points == 7 && T == 4) return launch_pt<7, 4>(pl, a, u, v, s, stream, occ);
   if (points == 13 && T == 2) return launch_pt<13, 2>(pl, a, u, v, s, stream, occ);
+  if (points == 13 && T == 4) return launch_pt<13, 4>(pl, a, u, v, s, stream, occ);
+  if (points == 25 && T == 2) return launch_pt<25, 2>(pl, a, u, v, s, stream, occ);
   return cudaErrorInvalidConfiguration;
 }
 
@@ -345,6 +362,8 @@ size_t tb_smem_bytes(int points, int T) {
   if (points == 7 && T == 2) return TbShape<7, 2, tb_stages<7, 2>()>::smem();
   if (points == 7 && T == 4) return TbShape<7, 4, tb_stages<7, 4>()>::smem();
   if (points == 13 && T == 2) return TbShape<13, 2, tb_stages<13, 2>()>::smem();
+  if (points == 13 && T == 4) return TbShape<13, 4, tb_stages<13, 4>()>::smem();
+  if (points == 25 && T == 2) return TbShape<25, 2, tb_stages<25, 2>()>::smem();
   return 0;
 }
 

@@ -58,9 +58,19 @@ struct Tma16Plan {
 // T=2 runs 26 rows (27 warps, 67 registers; 629 against 544 Gpts/s with 16
 // at 1024^3, the same bits), T=4 18 rows (568 against 531; 20 rows do not
 // fit in shared memory), 13 points T=2 18 rows (452 against 411; 20 rows cap
-// the registers at 80 and spill, 372).
+// the registers at 80 and spill, 372).  13 points T=4 and 25 points T=2 keep
+// 2R+1 planes of T levels in register queues (80 and 72 floats a lane): 15
+// rows make a 16-warp CTA whose threads may hold 128 registers.
 __host__ __device__ constexpr int tb_rows(int points, int T) {
-  return (points == 7 && T == 2) ? 26 : 18;
+  return (points == 7 && T == 2) ? 26 : (points == 25 || (points == 13 && T == 4)) ? 15 : 18;
+}
+// Columns of k margin either side of a temporally blocked tile's 128 level
+// columns: level t is exact in all but (t-1)R columns at either edge, so the
+// margin must be >= (T-1)R.  4 (tiles write 120 columns) while (T-1)R <= 4,
+// else 8 (112 columns: 13 points T=4, (T-1)R = 6).  A multiple of 4 floats,
+// so every TMA x coordinate stays 16-byte aligned.
+__host__ __device__ constexpr int tb_khalo(int points, int T) {
+  return (T - 1) * ((points == 25) ? 4 : (points == 13) ? 2 : 1) > 4 ? 8 : 4;
 }
 struct TbPlan {
   int T = 2, radius = 0, rows = 0, rows_out = 0;

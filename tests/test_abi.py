@@ -121,8 +121,9 @@ def test_plan_layout():
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", src=(8, 0, 0)), S.api.ERR_INVALID),
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", temporal_block=4), S.api.OK),
     ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", temporal_block=2), S.api.OK),
-    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", temporal_block=4), S.api.ERR_UNSUPPORTED),
-    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", temporal_block=2), S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", temporal_block=4), S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", temporal_block=2), S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", temporal_block=4), S.api.ERR_UNSUPPORTED),
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="ref", temporal_block=2), S.api.ERR_UNSUPPORTED),
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", temporal_block=3), S.api.ERR_INVALID),
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", storage="f16", temporal_block=2),

@@ -24,7 +24,7 @@ from tests.helpers import mode_r_inputs, rel_l2
 pytestmark = pytest.mark.gpu
 
 # temporal-blocking depths the library serves for the 13-point stencil
-TB13 = (1, 2)
+TB13 = (1, 2, 4)
 
 
 @pytest.mark.parametrize("points,n,steps", [(7, 256, 20), (25, 528, 200), (25, 1024, 20)])

@@ -3,8 +3,10 @@
 Bar: bit-identical to the same number of plain steps of the TMA kernel and
 to the oracle's fused flavour (the fused pass evaluates every level point
 with the single-step operation sequence), for step counts that mix fused
-passes with single steps.  Temporal blocking needs a zero halo; a non-zero
-halo is refused at upload.
+passes with single steps, for every depth served: 7 points T = 2, 4; 13
+points T = 2, 4 (tiles with 8 columns of k margin, 112 written); 25 points
+T = 2.  Temporal blocking needs a zero halo; a non-zero halo is refused at
+upload.
 """
 import numpy as np
 import pytest
@@ -15,7 +17,7 @@ from tests.helpers import halo_mask
 
 pytestmark = pytest.mark.gpu
 
-DEPTHS = [(7, 2), (7, 4), (13, 2)]
+DEPTHS = [(7, 2), (7, 4), (13, 2), (13, 4), (25, 2)]
 
 
 def _inputs(grid, seed):
@@ -114,7 +116,8 @@ def test_nonzero_halo_is_refused():
         assert e.value.status == S.api.ERR_UNSUPPORTED
 
 
-@pytest.mark.parametrize("points,T,rows", [(7, 2, 26), (7, 4, 18), (13, 2, 18), (7, 1, 0)])
+@pytest.mark.parametrize("points,T,rows", [(7, 2, 26), (7, 4, 18), (13, 2, 18), (13, 4, 15),
+                                           (25, 2, 15), (7, 1, 0)])
 def test_fused_tile_height_is_reported(points, T, rows):
     """st3d_info.tb_tile_j: the level-1 rows of a fused pass's tile (the
     height the plan's tensor maps and the kernel share), 0 without fusion."""
