@@ -305,7 +305,7 @@ def batch_run(S, steps, warmup, n=64):
         total = info.interior_points
         out["points"] = int(total)
         out["work_items_per_step"] = int(info.work_items)
-        for schedule in ("sequential", "persistent", "graph"):
+        for schedule in ("sequential", "persistent", "graph", "pipelined"):
             b.iterate(warmup, schedule)
             b.synchronize()
             l0 = b.info().launches
@@ -317,6 +317,7 @@ def batch_run(S, steps, warmup, n=64):
                              "ms_per_step": ms / steps,
                              "launches": int(b.info().launches - l0)}
     out["graph_vs_sequential"] = out["graph"]["value"] / out["sequential"]["value"]
+    out["pipelined_vs_sequential"] = out["pipelined"]["value"] / out["sequential"]["value"]
     # the autotuner's pick of unit length and schedule for this batch
     import tempfile
     from stencil3d_gb300 import autotune
@@ -471,6 +472,8 @@ def summary_of(result):
     if b:
         out["batch"] = {"seq": _r(b["sequential"]["value"]), "persistent": _r(b["persistent"]["value"]),
                         "graph": _r(b["graph"]["value"]), "graph_vs_seq": _r(b["graph_vs_sequential"], 3)}
+        if "pipelined" in b:
+            out["batch"]["pipelined"] = _r(b["pipelined"]["value"])
     for wl, r in (result.get("temporal_blocking") or {}).items():
         out["tb_" + wl] = {k: _r(e["value"]) for k, e in r.items() if isinstance(e, dict)}
         out["tb_" + wl]["steps"] = r["steps"]

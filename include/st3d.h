@@ -325,13 +325,20 @@ double st3d_ricker(double t, double f, double t0);
  *                          (grid, tile, chunk) items from a device work queue;
  *   ST3D_BATCH_GRAPH       the persistent schedule with the whole time loop
  *                          captured once in a CUDA graph (cached by step
- *                          count) and replayed. */
+ *                          count) and replayed;
+ *   ST3D_BATCH_PIPELINED   every step of the call in ONE persistent launch:
+ *                          a per-(step, grid) counter of finished work items
+ *                          lets a grid start its next step as soon as its own
+ *                          previous step is done (bounded device waits), so
+ *                          no step drains the GPU.  steps x work items must
+ *                          stay below 2^31. */
 typedef struct st3d_batch st3d_batch;
 
 typedef enum st3d_batch_schedule {
   ST3D_BATCH_SEQUENTIAL = 0,
   ST3D_BATCH_PERSISTENT = 1,
-  ST3D_BATCH_GRAPH = 2
+  ST3D_BATCH_GRAPH = 2,
+  ST3D_BATCH_PIPELINED = 3
 } st3d_batch_schedule;
 
 typedef struct st3d_batch_info {

@@ -78,8 +78,9 @@ class BatchInfo(C.Structure):
                 ("reserved", C.c_int32 * 8)]
 
 
-BATCH_SEQUENTIAL, BATCH_PERSISTENT, BATCH_GRAPH = 0, 1, 2
-_SCHEDULES = {"sequential": BATCH_SEQUENTIAL, "persistent": BATCH_PERSISTENT, "graph": BATCH_GRAPH}
+BATCH_SEQUENTIAL, BATCH_PERSISTENT, BATCH_GRAPH, BATCH_PIPELINED = 0, 1, 2, 3
+_SCHEDULES = {"sequential": BATCH_SEQUENTIAL, "persistent": BATCH_PERSISTENT, "graph": BATCH_GRAPH,
+              "pipelined": BATCH_PIPELINED}
 
 _lib = None
 
@@ -361,7 +362,8 @@ class Batch:
     """Many independent grids (FP32 wave form, 7/13/25 points) advancing
     together: ``Batch(grids, points, dt=..., srcs=...)``; ``context(i)`` is a
     Stencil view of grid i for upload/download/fill/norms; ``iterate(n,
-    schedule)`` with schedule "sequential", "persistent" or "graph"."""
+    schedule)`` with schedule "sequential", "persistent", "graph" or
+    "pipelined"."""
 
     def __init__(self, grids, points, dt=None, srcs=None, **kw):
         n = len(grids)

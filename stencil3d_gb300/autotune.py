@@ -3,7 +3,8 @@
 device, and keeps the choice in a JSON cache.
 
 For a batch of grids (``tune_batch``) the knobs are the planes per work
-unit and the schedule (CUDA graph or plain persistent launches).
+unit and the schedule (CUDA graph, plain persistent launches, or one
+pipelined launch per call).
 
 The knobs are the ``st3d_opts`` fields that change how the work is tiled,
 never what is computed: the kernel (TMA pipeline or plain), tile rows
@@ -166,7 +167,7 @@ def batch_candidates():
     queue, longer ones re-read fewer warm-up planes; 512 is a whole column
     of every grid up to 512 planes) and the schedule."""
     return [{"ichunk": ic, "schedule": sch} for ic in (32, 64, 128, 256, 512)
-            for sch in ("graph", "persistent")]
+            for sch in ("graph", "persistent", "pipelined")]
 
 
 def measure_batch_device(grids, points, cand, dts=None, srcs=None, steps=20, warmup=3):

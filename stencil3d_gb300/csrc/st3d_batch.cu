@@ -15,6 +15,20 @@
 // time loop (a queue reset and a launch per step) can be captured in a CUDA
 // graph and replayed.  The baseline schedule launches the single-grid kernel
 // once per grid per step.
+//
+// The pipelined schedule runs every step of a call in ONE persistent launch:
+// the queue runs over (step, item) in step-major order, and a per-(step,
+// grid) counter of finished items orders the steps of each grid.  Before a
+// CTA loads an item of step t > 0 its producer waits (bounded) until every
+// item of step t - 1 of the same grid has finished: step t reads U^t, which
+// step t - 1 wrote, and overwrites U^{t-1}, which step t - 1 read with its
+// halo.  Grids do not wait for one another, so the tail of one step (the
+// smallest grids: the item order puts the largest first) overlaps the start
+// of the next instead of draining the GPU at a kernel boundary.  Finishing an
+// item: the consumer warps meet at a named barrier, then one thread fences
+// (generic and async proxy) and adds to the counter with release semantics;
+// the waiting producer reads it with acquire semantics and fences the async
+// proxy before its TMA loads.
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -64,7 +78,9 @@ struct BatchArgs {
   int n_grids;
   int* head;
   const float* amps;  // [step][grid]
-  int step;           // step within the call
+  int step;           // step within the call of the launch's first step
+  int nsteps;         // steps of this launch (1, or all steps of a pipelined call)
+  int* done;          // pipelined: finished items per (step, grid); nullptr otherwise
   uint64_t timeout_ns;
   uint32_t* status;
 };
@@ -72,15 +88,43 @@ struct BatchArgs {
 struct BStage {
   int grid;  // -1: no more work
   int unit;
-  int pad[2];
+  int step;  // step within the call
+  int pad;
 };
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_gpu_add(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Waits until *ctr reaches `target` (acquire); false after `limit_ns`.
+__device__ bool wait_counter(const int* ctr, int target, uint64_t limit_ns) {
+  if (ld_acquire_gpu(ctr) >= target) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 1; it < (1u << 26); ++it) {
+    __nanosleep(it < 64 ? 32 : 256);
+    if (ld_acquire_gpu(ctr) >= target) return true;
+    if ((it & 15u) == 0 && global_ns() - t0 > limit_ns) return false;
+  }
+  return false;
+}
 
 constexpr int kUSlot = (kTmaUKW * (kBTJ + 2 * kBRmax) + 31) / 32 * 32;  // floats
 constexpr int kVSlot = kTmaTK * kBTJ;                                   // floats
 constexpr int kNU = kBNV + kBRmax;
 
 size_t batch_smem_bytes() {
-  return ((size_t)kNU * kUSlot + 2 * (size_t)kBNV * kVSlot) * 4 + 2 * kBNV * 8 + kBNV * sizeof(BStage) + 128;
+  return ((size_t)kNU * kUSlot + 2 * (size_t)kBNV * kVSlot) * 4 + 2 * kBNV * 8 + kBNV * sizeof(BStage) +
+         16 + 128;
 }
 
 // The consumer side of one work unit (the single-grid kernel's consumer loop
@@ -93,7 +137,7 @@ static_assert((kNTK + 2 * kTmaKHalo) * (kNTJ + 2 * kBRmax) <= kUSlot && kNTK * k
               "narrow tile does not fit the slots");
 template <int P>
 __device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid& G, int gi, int unit,
-                                             uint32_t h0, float* ur, float* vr, float* sr,
+                                             int step, uint32_t h0, float* ur, float* vr, float* sr,
                                              uint64_t* full, uint64_t* empty, int warp, int lane) {
   constexpr int R = (P == 25) ? 4 : (P == 13) ? 2 : 1;
   constexpr int QN = 2 * R + 1;
@@ -115,10 +159,10 @@ __device__ __forceinline__ bool consume_unit(const BatchArgs& a, const BatchGrid
   const int ib = min(ia + G.ichunk, g.xs);
   const int nsteps = (ib - ia) + 2 * R;
   const bool row_ok = j < g.ys;
-  const int ub = G.cur0 ^ (a.step & 1);
+  const int ub = G.cur0 ^ (step & 1);
   float* vout = G.buf[ub ^ 1];
   float* vrow = vout + g.org + (long long)j * g.sj + k;
-  const float amp = (G.src_i >= 0) ? a.amps[(size_t)a.step * a.n_grids + gi] : 0.0f;
+  const float amp = (G.src_i >= 0) ? a.amps[(size_t)step * a.n_grids + gi] : 0.0f;
   float4 q[QN];
   for (int n0 = 0; n0 < nsteps; n0 += QN) {
 #pragma unroll
@@ -208,10 +252,12 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
   uint64_t* full = reinterpret_cast<uint64_t*>(sr + kBNV * kVSlot);
   uint64_t* empty = full + kBNV;
   BStage* info = reinterpret_cast<BStage*>(empty + kBNV);
+  unsigned* finished = reinterpret_cast<unsigned*>(info + kBNV);  // warps done, all items
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
+    *finished = 0u;
     for (int s = 0; s < kBNV; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kBTJ);
@@ -226,9 +272,10 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
     if (lane != 0) return;
     uint32_t h = 0;
     bool ok = true;
+    const int last = a.total_items * a.nsteps;
     while (ok) {
-      const int item = atomicAdd(a.head, 1);
-      const bool stop = item >= a.total_items;
+      const int x = atomicAdd(a.head, 1);
+      const bool stop = x >= last;
       const int stage0 = (int)(h % kBNV);
       if (stop) {
         // hand the consumers a stop record through the pipeline
@@ -241,10 +288,22 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
         mbar_arrive(&full[stage0]);
         break;
       }
-      const int2 it = a.items[item];
+      const int tl = x / a.total_items;  // step of the launch
+      const int step = a.step + tl;
+      const int2 it = a.items[x - tl * a.total_items];
       const BatchGrid& G = a.grids[it.x];
       const int R = G.R;
       const int unit = it.y;
+      if (a.done && tl > 0) {
+        // every item of the grid's previous step has finished (acquire);
+        // then order the async proxy (TMA) after it
+        if (!wait_counter(a.done + (size_t)(tl - 1) * a.n_grids + it.x, G.units, a.timeout_ns)) {
+          atomicExch(a.status, (uint32_t)kDevTimeoutDep);
+          ok = false;
+          break;
+        }
+        fence_proxy_async_global();
+      }
       const int ic = unit / G.ntjk;
       const int rem = unit - ic * G.ntjk;
       const int jt = rem / G.ntk;
@@ -254,7 +313,7 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
       const int ia = ic * G.ichunk;
       const int ib = min(ia + G.ichunk, G.g.xs);
       const int nsteps = (ib - ia) + 2 * R;
-      const int ub = G.cur0 ^ (a.step & 1);
+      const int ub = G.cur0 ^ (step & 1);
       const CUtensorMap* umap = &a.maps[G.map_base + ub];
       const CUtensorMap* vmap = &a.maps[G.map_base + 2 + (ub ^ 1)];
       const CUtensorMap* smap = &a.maps[G.map_base + 4];
@@ -270,6 +329,7 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
         }
         info[stage].grid = it.x;
         info[stage].unit = unit;
+        info[stage].step = step;
         const bool has_vs = n >= 2 * R;
         mbar_arrive_expect_tx(&full[stage], ubytes + (has_vs ? 2 * vbytes : 0u));
         tma_load_3d(ur + (h % kNU) * kUSlot, umap, &full[stage], G.g.pk + k0 - kTmaKHalo,
@@ -306,11 +366,26 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
       nsteps = (min(ia + G.ichunk, G.g.xs) - ia) + 2 * G.R;
     }
     switch (G.P) {
-      case 7: ok = consume_unit<7>(a, G, st.grid, st.unit, h, ur, vr, sr, full, empty, warp, lane); break;
-      case 13: ok = consume_unit<13>(a, G, st.grid, st.unit, h, ur, vr, sr, full, empty, warp, lane); break;
-      default: ok = consume_unit<25>(a, G, st.grid, st.unit, h, ur, vr, sr, full, empty, warp, lane); break;
+      case 7: ok = consume_unit<7>(a, G, st.grid, st.unit, st.step, h, ur, vr, sr, full, empty, warp, lane); break;
+      case 13: ok = consume_unit<13>(a, G, st.grid, st.unit, st.step, h, ur, vr, sr, full, empty, warp, lane); break;
+      default: ok = consume_unit<25>(a, G, st.grid, st.unit, st.step, h, ur, vr, sr, full, empty, warp, lane); break;
     }
     if (!ok) return;
+    if (a.done) {
+      // This warp's stores of the item are done; the last warp of the CTA to
+      // get here publishes the item (a counter in shared memory, no blocking
+      // barrier: a warp that gave up on a wait never stalls the others).
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence();
+        const unsigned old = atomicAdd(finished, 1u);
+        if (old % kBTJ == kBTJ - 1) {
+          __threadfence();
+          fence_proxy_async_global();
+          red_release_gpu_add(a.done + (size_t)(st.step - a.step) * a.n_grids + st.grid, 1);
+        }
+      }
+    }
     h += (uint32_t)nsteps;
   }
 }
@@ -332,6 +407,8 @@ struct st3d_batch {
   int2* d_items = nullptr;
   int* d_head = nullptr;  // one queue head per step of the largest call
   int heads = 0;
+  int* d_done = nullptr;  // pipelined schedule: finished items per (step, grid)
+  size_t done_cap = 0;
   float* d_amps = nullptr;
   size_t amps_cap = 0;
   float* h_amps = nullptr;  // pinned staging of the amplitudes
@@ -383,6 +460,12 @@ int ensure_steps(st3d_batch* b, uint32_t steps) {
     b->heads = (int)steps;
     destroy_graphs(b);
   }
+  if (need > b->done_cap) {
+    if (b->d_done) cudaFree(b->d_done);
+    b->d_done = nullptr;
+    B_CUDA(cudaMalloc(&b->d_done, need * sizeof(int)));
+    b->done_cap = need;
+  }
   return ST3D_OK;
 }
 
@@ -422,11 +505,38 @@ int enqueue_persistent(st3d_batch* b, uint32_t steps) {
     a.head = b->d_head + t;
     a.amps = b->d_amps;
     a.step = (int)t;
+    a.nsteps = 1;
+    a.done = nullptr;
     a.timeout_ns = 4000000000ull;
     a.status = b->d_status;
     k_batch<<<b->ctas, (kBTJ + 1) * 32, b->smem, b->stream>>>(a);
     B_CUDA(cudaGetLastError());
   }
+  return ST3D_OK;
+}
+
+// All steps of the call in one persistent launch: one queue over (step,
+// item) and the per-(step, grid) counters of finished items, both cleared
+// first.
+int enqueue_pipelined(st3d_batch* b, uint32_t steps) {
+  const size_t n = b->ctx.size();
+  B_CUDA(cudaMemsetAsync(b->d_head, 0, sizeof(int), b->stream));
+  B_CUDA(cudaMemsetAsync(b->d_done, 0, (size_t)steps * n * sizeof(int), b->stream));
+  BatchArgs a;
+  a.grids = b->d_grids;
+  a.maps = b->d_maps;
+  a.items = b->d_items;
+  a.total_items = b->total_items;
+  a.n_grids = (int)n;
+  a.head = b->d_head;
+  a.amps = b->d_amps;
+  a.step = 0;
+  a.nsteps = (int)steps;
+  a.done = b->d_done;
+  a.timeout_ns = 4000000000ull;
+  a.status = b->d_status;
+  k_batch<<<b->ctas, (kBTJ + 1) * 32, b->smem, b->stream>>>(a);
+  B_CUDA(cudaGetLastError());
   return ST3D_OK;
 }
 
@@ -582,6 +692,7 @@ int st3d_batch_destroy(st3d_batch* b) {
   if (b->d_maps) cudaFree(b->d_maps);
   if (b->d_items) cudaFree(b->d_items);
   if (b->d_head) cudaFree(b->d_head);
+  if (b->d_done) cudaFree(b->d_done);
   if (b->d_amps) cudaFree(b->d_amps);
   if (b->h_amps) cudaFreeHost(b->h_amps);
   if (b->d_status) cudaFree(b->d_status);
@@ -626,10 +737,19 @@ int st3d_batch_iterate(st3d_batch* b, uint32_t steps, int schedule) {
     b->launches += (uint64_t)steps * b->ctx.size();
     return ST3D_OK;
   }
-  if (schedule != ST3D_BATCH_PERSISTENT && schedule != ST3D_BATCH_GRAPH)
+  if (schedule != ST3D_BATCH_PERSISTENT && schedule != ST3D_BATCH_GRAPH &&
+      schedule != ST3D_BATCH_PIPELINED)
     return bfail(ST3D_ERR_INVALID, "unknown batch schedule");
+  if (schedule == ST3D_BATCH_PIPELINED && (uint64_t)steps * b->total_items > 0x7fffffffull)
+    return bfail(ST3D_ERR_UNSUPPORTED, "too many steps for one pipelined launch (steps x items < 2^31)");
   if ((rc = ensure_steps(b, steps)) != ST3D_OK) return rc;
   if ((rc = stage_call(b, steps)) != ST3D_OK) return rc;
+  if (schedule == ST3D_BATCH_PIPELINED) {
+    if ((rc = enqueue_pipelined(b, steps)) != ST3D_OK) return rc;
+    b->launches += 1;
+    advance(b, steps);
+    return ST3D_OK;
+  }
   if (schedule == ST3D_BATCH_PERSISTENT) {
     if ((rc = enqueue_persistent(b, steps)) != ST3D_OK) return rc;
   } else {

@@ -135,6 +135,7 @@ enum DeviceStatus : uint32_t {
   kDevOk = 0,
   kDevTimeoutFull = 1,
   kDevTimeoutEmpty = 2,
+  kDevTimeoutDep = 3,   // a wait for another CTA's finished work (batch, pipelined)
 };
 
 // Records a formatted message for st3d_last_error() and returns `status`.

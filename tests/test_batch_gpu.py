@@ -1,8 +1,9 @@
 """GPU tests of the batching form: independent grids of uneven sizes and
 stencil orders advancing in one persistent launch per step (device work
-queue), optionally replayed from a CUDA graph, against the sequential
-schedule and the oracle.  All schedules run the same arithmetic, so the
-fields must agree bit for bit."""
+queue), optionally replayed from a CUDA graph, or in one launch for all
+steps of a call (the pipelined schedule: per-grid step counters), against
+the sequential schedule and the oracle.  All schedules run the same
+arithmetic, so the fields must agree bit for bit."""
 import numpy as np
 import pytest
 
@@ -45,7 +46,7 @@ def _run(specs, steps_list, schedule, seed):
     return out, inputs, info
 
 
-@pytest.mark.parametrize("schedule", ["persistent", "graph"])
+@pytest.mark.parametrize("schedule", ["persistent", "graph", "pipelined"])
 def test_batch_schedules_match_sequential_and_oracle(schedule):
     specs = _grids(7, 9)
     steps_list = [5, 4, 4]  # odd first call: buffer parity and graph reuse
@@ -73,6 +74,20 @@ def test_batch_counts_one_launch_per_step():
     assert info.launches == 6
     _, _, info = _run(specs, [6], "sequential", 1)
     assert info.launches == 6 * 5
+    _, _, info = _run(specs, [6, 3], "pipelined", 1)
+    assert info.launches == 2  # one launch per call
+
+
+def test_pipelined_many_steps_few_grids():
+    """Two grids of very different sizes over many steps in one launch: the
+    small grid runs steps ahead of the large one while each grid's steps stay
+    in order (per-grid counters); same bits as the sequential schedule."""
+    specs = [((96, 70, 140, 4, 4, 4), 25, (40, 30, 70)), ((9, 7, 20, 4, 4, 4), 7, (4, 3, 10))]
+    seq, _, _ = _run(specs, [17], "sequential", 5)
+    got, _, _ = _run(specs, [17], "pipelined", 5)
+    for (ua, va), (ub, vb) in zip(got, seq):
+        np.testing.assert_array_equal(ua, ub)
+        np.testing.assert_array_equal(va, vb)
 
 
 def test_batch_rejects_other_forms():

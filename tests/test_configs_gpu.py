@@ -87,7 +87,7 @@ def test_batch_full_workload_graph_equals_sequential():
     srcs = [sp for _, _, sp in specs]
     batches = []
     try:
-        for schedule in ("sequential", "graph"):
+        for schedule in ("sequential", "graph", "pipelined"):
             b = S.Batch(grids, pts, dt=dts, srcs=srcs)
             batches.append(b)
             for i in range(len(grids)):
@@ -97,11 +97,12 @@ def test_batch_full_workload_graph_equals_sequential():
                 st.fill(S.FIELD_S, S.FILL_CONST, 0, 0.0)
             b.iterate(5, schedule)
             b.synchronize()
-        for i in range(len(grids)):
-            a, c = batches[0].context(i), batches[1].context(i)
-            for field in (S.FIELD_U, S.FIELD_V):
-                d2, b2, dm, bm = c.norms(field, a, field)
-                assert b2 > 0 and d2 == 0.0, (i, field)
+        for other in batches[1:]:
+            for i in range(len(grids)):
+                a, c = batches[0].context(i), other.context(i)
+                for field in (S.FIELD_U, S.FIELD_V):
+                    d2, b2, dm, bm = c.norms(field, a, field)
+                    assert b2 > 0 and d2 == 0.0, (i, field)
     finally:
         for b in batches:
             b.close()
