@@ -61,8 +61,9 @@ def candidates(points, mode, storage, zero_halo=False):
         for ic in (0, 64, 256):
             out.append({"kernel": "tma", "tile_j": tj, "stages": nv, "ichunk": ic})
     out.append({"kernel": "simple", "ichunk": 64})
-    if zero_halo and mode == "wave" and points in (7, 13):
-        for T in ((2, 4) if points == 7 else (2,)):
+    if zero_halo and mode == "wave":
+        # the fused depths the library serves: (T - 1) * R <= 8
+        for T in ((2, 4) if points in (7, 13) else (2,)):
             for ic in (0, 64):
                 out.append({"kernel": "tma", "temporal_block": T, "ichunk": ic})
     return out

@@ -56,6 +56,7 @@ constexpr int kBTJ = 12;
 constexpr int kNTJ = 24;
 constexpr int kNTK = 64;
 constexpr int kBNV = 6;  // pipeline stages (4 measured 335.9, 6 362.4, 8 359.8 Gpts/s)
+constexpr int kItemSlots = 2 * kBNV;  // pipelined schedule: item completion counters per CTA
 constexpr int kBRmax = 4;
 
 struct BatchGrid {
@@ -124,7 +125,7 @@ constexpr int kNU = kBNV + kBRmax;
 
 size_t batch_smem_bytes() {
   return ((size_t)kNU * kUSlot + 2 * (size_t)kBNV * kVSlot) * 4 + 2 * kBNV * 8 + kBNV * sizeof(BStage) +
-         16 + 128;
+         kItemSlots * sizeof(unsigned) + 128;
 }
 
 // The consumer side of one work unit (the single-grid kernel's consumer loop
@@ -252,12 +253,12 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
   uint64_t* full = reinterpret_cast<uint64_t*>(sr + kBNV * kVSlot);
   uint64_t* empty = full + kBNV;
   BStage* info = reinterpret_cast<BStage*>(empty + kBNV);
-  unsigned* finished = reinterpret_cast<unsigned*>(info + kBNV);  // warps done, all items
+  unsigned* finished = reinterpret_cast<unsigned*>(info + kBNV);  // warps done, per item slot
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    *finished = 0u;
+    for (int q = 0; q < kItemSlots; ++q) finished[q] = 0u;
     for (int s = 0; s < kBNV; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kBTJ);
@@ -349,6 +350,7 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
 
   // ---------------- consumers ----------------
   uint32_t h = 0;
+  uint32_t seq = 0;  // items this warp has taken (the same sequence in every warp)
   while (true) {
     const int stage = (int)(h % kBNV);
     if (!mbar_wait_bounded(&full[stage], (h / kBNV) & 1u, a.timeout_ns)) {
@@ -373,19 +375,25 @@ __global__ void __launch_bounds__((kBTJ + 1) * 32, 1) k_batch(const BatchArgs a)
     if (!ok) return;
     if (a.done) {
       // This warp's stores of the item are done; the last warp of the CTA to
-      // get here publishes the item (a counter in shared memory, no blocking
-      // barrier: a warp that gave up on a wait never stalls the others).
+      // get here publishes the item.  Every warp takes the CTA's items in the
+      // same order, so the item's sequence number picks its counter; a warp
+      // runs at most kBNV stages (so at most kBNV items) ahead of the slowest,
+      // hence kItemSlots > kBNV counters never mix two items.  No blocking
+      // barrier: a warp that gave up on a wait never stalls the others.
       __syncwarp();
       if (lane == 0) {
+        unsigned* slot = finished + (seq % kItemSlots);
         __threadfence();
-        const unsigned old = atomicAdd(finished, 1u);
-        if (old % kBTJ == kBTJ - 1) {
+        const unsigned old = atomicAdd(slot, 1u);
+        if (old == kBTJ - 1) {
+          atomicExch(slot, 0u);  // free for item seq + kItemSlots
           __threadfence();
           fence_proxy_async_global();
           red_release_gpu_add(a.done + (size_t)(st.step - a.step) * a.n_grids + st.grid, 1);
         }
       }
     }
+    ++seq;
     h += (uint32_t)nsteps;
   }
 }

@@ -31,7 +31,9 @@ def test_temporal_blocking_only_on_request():
     fused = autotune.candidates(13, "wave", "f32", zero_halo=True)
     assert not any(c.get("temporal_block", 1) > 1 for c in plain)
     assert any(c.get("temporal_block", 1) == 2 for c in fused)
-    assert not any(c.get("temporal_block", 1) == 4 for c in fused)  # (T-1)R > 4 for 13 points
+    assert any(c.get("temporal_block", 1) == 4 for c in fused)  # (T-1)R = 6 <= 8
+    deep = autotune.candidates(25, "wave", "f32", zero_halo=True)
+    assert {c.get("temporal_block", 1) for c in deep} == {1, 2}  # 25 points: T=4 is (T-1)R = 12
 
 
 def test_tune_picks_the_fastest_and_caches(tmp_path):

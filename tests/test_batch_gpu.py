@@ -25,13 +25,13 @@ def _grids(seed, n):
     return out
 
 
-def _run(specs, steps_list, schedule, seed):
+def _run(specs, steps_list, schedule, seed, **kw):
     grids = [S.Grid(*g) for g, _, _ in specs]
     pts = [p for _, p, _ in specs]
     dts = [1e-3 if p == 7 else 5e-4 for p in pts]
     srcs = [s for _, _, s in specs]
     inputs = [wave_inputs(g, seed + i) for i, (g, _, _) in enumerate(specs)]
-    with S.Batch(grids, pts, dt=dts, srcs=srcs) as b:
+    with S.Batch(grids, pts, dt=dts, srcs=srcs, **kw) as b:
         for i, (v, s, u) in enumerate(inputs):
             b.context(i).upload(v, s, u)
         for n in steps_list:
@@ -96,3 +96,17 @@ def test_batch_rejects_other_forms():
     h = S.api.C.c_void_p()
     rc = S.lib().st3d_batch_create(1, (S.api.GridDesc * 1)(g.desc()), opts, S.api.C.byref(h))
     assert rc == S.api.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("ichunk", [1, 3, 32])
+def test_pipelined_short_units(ichunk):
+    """Units of a few planes: a consumer warp can finish a short unit while
+    another warp of its CTA still works on the previous one, so completions
+    must be counted per unit; every call ends without a timed-out wait and
+    with the sequential schedule's bits."""
+    specs = _grids(11, 7)
+    seq, _, _ = _run(specs, [6, 5], "sequential", 9, ichunk=ichunk)
+    got, _, _ = _run(specs, [6, 5], "pipelined", 9, ichunk=ichunk)
+    for (ua, va), (ub, vb) in zip(got, seq):
+        np.testing.assert_array_equal(ua, ub)
+        np.testing.assert_array_equal(va, vb)
