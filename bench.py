@@ -547,10 +547,25 @@ def cpu_wave_sample(wl, u, v, target_s, threads):
     t0 = time.perf_counter()
     O.iterate_wave(u, v, s, grid, points, n, c0, c1, c2, src=src, amps=amps[1:], fma=False)
     el = time.perf_counter() - t0
-    return {"value": xs * ys * zs * n / el / 1e9, "unit": "Gpts/s", "cores": threads,
-            "kind": "port",
-            "sample": "%d full %s leapfrog steps (%.1f s) of the oracle's C restatement, "
-                      "OpenMP %d threads" % (n, wl, el, threads)}
+    out = {"value": xs * ys * zs * n / el / 1e9, "unit": "Gpts/s", "cores": threads,
+           "kind": "port",
+           "sample": "%d full %s leapfrog steps (%.1f s) of the oracle's C restatement, "
+                     "OpenMP %d threads" % (n, wl, el, threads)}
+    # the reference's own update (mode R) restated: the plain flavour is bit
+    # for bit the reference's compiled stencil_*_ref_1 over its jk-blocked
+    # traversal; fields as they are (the timing does not depend on them)
+    s[...] = 1.0
+    t0 = time.perf_counter()
+    O.iterate_ref(v, s, u, grid, points, 1, fma=False)
+    one = time.perf_counter() - t0
+    nr = max(1, min(50, int(0.5 * target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    O.iterate_ref(v, s, u, grid, points, nr, fma=False)
+    el = time.perf_counter() - t0
+    out["mode_r"] = {"value": xs * ys * zs * nr / el / 1e9, "unit": "Gpts/s",
+                     "sample": "%d mode R steps (%.1f s) of %s, the reference's update restated, "
+                               "OpenMP %d threads" % (nr, el, wl, threads)}
+    return out
 
 
 def host_threads():
