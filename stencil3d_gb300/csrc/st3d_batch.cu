@@ -25,10 +25,15 @@
 // halo.  Grids do not wait for one another, so the tail of one step (the
 // smallest grids: the item order puts the largest first) overlaps the start
 // of the next instead of draining the GPU at a kernel boundary.  Finishing an
-// item: the consumer warps meet at a named barrier, then one thread fences
-// (generic and async proxy) and adds to the counter with release semantics;
-// the waiting producer reads it with acquire semantics and fences the async
-// proxy before its TMA loads.
+// item: each consumer warp's lane 0 fences and counts the warp in a shared-
+// memory counter of the item (one per item sequence number, modulo twice the
+// pipeline depth), and the last warp fences (generic and async proxy) and
+// adds to the global counter with release semantics; the waiting producer
+// reads it with acquire semantics and fences the async proxy before its TMA
+// loads.  All waits are bounded and report through the status word: a
+// consumer warp whose wait gave up returns (the call's results are then
+// void), the producer's own bounded waits then give up too, and its drain
+// waits (bounded) for the stages it issued last.
 #include <algorithm>
 #include <cstring>
 #include <map>

@@ -29,8 +29,16 @@
 //     the left and right float4).  v and s come from their stage slots; the
 //     new v leaves with a 128-bit coalesced store.
 // Every wait is bounded (mbar_wait_bounded): on timeout the kernel records
-// the reason in a device status word and returns, so a broken pipeline ends
-// as an error code instead of a hung GPU.
+// the reason in a device status word, so a broken pipeline ends as an error
+// code instead of a hung GPU.  A consumer warp whose wait gave up does not
+// return: it stops waiting but keeps stepping and arriving on the stages'
+// empty barriers (its results are void; the status word says so), so the
+// producer keeps going to the end of its units and its drain waits for the
+// copies it issued last -- a CTA that left with bulk copies still in flight
+// into its shared memory could fault the GPU (a mis-sized transaction count
+// once did, with Xid 43).  Only a copy that never lands at all, which no
+// kernel code can repair, ends the drain's bounded waits with copies in
+// flight.
 //
 // Arithmetic: the same operation sequence as the direct-load kernel and the
 // oracle's fma flavour (see st3d_kernels_simple.cu), on packed FP32 pairs
@@ -137,6 +145,7 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
   // ---------------- consumers ----------------
   const int r = warp;
   uint32_t h = 0;
+  bool failed = false;
   float4 q[QN];
   for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
     const int ic = unit / ntjk;
@@ -157,9 +166,9 @@ __global__ void __launch_bounds__((TJ + 1) * 32, 1)
         if (n >= nsteps) break;
         const uint32_t hh = h + (uint32_t)n;
         const int stage = (int)(hh % NV);
-        if (!mbar_wait_bounded(&full[stage], (hh / NV) & 1u, timeout_ns)) {
+        if (!failed && !mbar_wait_bounded(&full[stage], (hh / NV) & 1u, timeout_ns)) {
           atomicExch(status, (uint32_t)kDevTimeoutFull);
-          return;
+          failed = true;
         }
         q[ph] = *reinterpret_cast<const float4*>(ur + (hh % NU) * USLOT + (r + R) * UKW +
                                                  kTmaKHalo + 4 * lane);
