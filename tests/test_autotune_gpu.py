@@ -63,4 +63,4 @@ def test_batch_tuner_end_to_end(tmp_path):
     pts = [7, 13, 25]
     best = autotune.tune_batch(grids, pts, dts=[1e-3, 5e-4, 5e-4], steps=3,
                                cache=str(tmp_path / "tune.json"))
-    assert best["gpts"] > 0 and best["opts"]["schedule"] in ("graph", "persistent")
+    assert best["gpts"] > 0 and best["opts"]["schedule"] in ("graph", "persistent", "pipelined")
