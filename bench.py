@@ -522,7 +522,8 @@ def e2e_run(S, st, g, calls, iters):
     d2h = 2 * xs * ys * (zs + 2 * g.zhalo) * 4
     return {"value": pts * iters / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "host_path": {0: "auto", 1: "staged", 2: "direct", 3: "strided"}[st.info().host_path],
+            "host_path": {0: "auto", 1: "staged", 2: "direct", 3: "strided",
+                          4: "streamed"}[st.info().host_path],
             "step": "one ITERATE-equivalent call (st3d_iterate_host) of %d time steps" % iters,
             "ms_per_call": ms, "phases": phases,
             "h2d_gbs": h2d / (phases["upload_ms"] * 1e-3) / 1e9,
@@ -694,12 +695,16 @@ def run_gb300(args, dist):
         e2e["value"] = dist.world * e2e["value"] if dist.world > 1 else e2e["value"]
         result["e2e"] = e2e
     st.close()
-    if args.e2e_calls > 0 and result["e2e"]["host_path"] == "direct":
-        # the same calls through the staging buffer, for comparison
-        g2, st2 = make_stencil(S, args.workload, "f32", args.kernel, host_path=S.api.HOST_STAGED)
-        e2s, _ = e2e_run(S, st2, g2, args.e2e_calls, args.e2e_iters)
-        st2.close()
-        result["e2e"]["staged"] = {k: e2s[k] for k in ("value", "ms_per_call", "phases", "h2d_gbs",
+    if args.e2e_calls > 0 and result["e2e"]["host_path"] in ("direct", "streamed"):
+        # the same calls phase by phase (upload, steps, download) on the
+        # direct path and through the staging buffer, for comparison
+        for name, hp in (("direct", S.api.HOST_DIRECT), ("staged", S.api.HOST_STAGED)):
+            if name == result["e2e"]["host_path"]:
+                continue
+            g2, st2 = make_stencil(S, args.workload, "f32", args.kernel, host_path=hp)
+            e2s, _ = e2e_run(S, st2, g2, args.e2e_calls, args.e2e_iters)
+            st2.close()
+            result["e2e"][name] = {k: e2s[k] for k in ("value", "ms_per_call", "phases", "h2d_gbs",
                                                       "d2h_gbs", "host_path")}
 
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and host is not None:

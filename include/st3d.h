@@ -114,12 +114,20 @@ typedef struct st3d_grid_desc {
  * arrays (cudaMallocHost, cudaHostAlloc, cudaHostRegister, st3d_host_alloc)
  * that lie inside one allocation.  AUTO takes DIRECT where it applies.
  * STRIDED: a 3-D strided copy, used when the host k halo exceeds the device
- * row pad. */
+ * row pad.  STREAMED (st3d_iterate_host only): the DIRECT path with the
+ * transfers and the steps overlapped in one launch -- CTAs copying planes of
+ * u, v and s in while the others step the planes already in, as a wavefront
+ * over chunks of `ichunk` planes along i (16 when 0), and copying the final
+ * planes out as they are done; the same bits as the phase-by-phase call.
+ * AUTO takes it for FP32 contexts on the TMA kernel's default tiles without
+ * temporal blocking when v, s and u are pinned (asking for STREAMED where it
+ * does not apply runs DIRECT). */
 typedef enum st3d_host_path {
   ST3D_HOST_AUTO = 0,
   ST3D_HOST_STAGED = 1,
   ST3D_HOST_DIRECT = 2,
-  ST3D_HOST_STRIDED = 3
+  ST3D_HOST_STRIDED = 3,
+  ST3D_HOST_STREAMED = 4
 } st3d_host_path;
 
 typedef struct st3d_opts {

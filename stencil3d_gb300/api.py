@@ -23,7 +23,7 @@ F32, F64, F16, BF16, F16_HILO, F16_HL = 0, 1, 2, 3, 4, 5
 KERNEL_AUTO, KERNEL_SIMPLE, KERNEL_TMA = 0, 1, 2
 FIELD_U, FIELD_V, FIELD_S = 0, 1, 2
 FILL_CONST, FILL_UNIFORM, FILL_BLOBS = 0, 1, 2
-HOST_AUTO, HOST_STAGED, HOST_DIRECT, HOST_STRIDED = 0, 1, 2, 3
+HOST_AUTO, HOST_STAGED, HOST_DIRECT, HOST_STRIDED, HOST_STREAMED = 0, 1, 2, 3, 4
 
 _MODES = {"ref": MODE_REF, "wave": MODE_WAVE}
 _STORAGES = {"f32": F32, "f64": F64, "f16": F16, "bf16": BF16, "f16_hilo": F16_HILO, "f16_hl": F16_HL}

@@ -9,6 +9,7 @@
 // CUDA stream.
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -781,6 +782,180 @@ int plan_tb(st3d_ctx* c, int sm_count) {
   return ST3D_OK;
 }
 
+// The streamed drop-in call (st3d_stream.cu): upload, `iterations` steps and
+// download in one cooperative launch.  *done = false (and nothing enqueued)
+// where it does not apply; the caller then runs the phases one by one.
+int iterate_host_streamed(st3d_ctx* c, void* v, const void* s, void* u, uint32_t iterations,
+                          bool* done) {
+  *done = false;
+  const int hp = c->opts.host_path;
+  if (hp != ST3D_HOST_AUTO && hp != ST3D_HOST_STREAMED) return ST3D_OK;
+  if (iterations < 1 || c->opts.storage != ST3D_F32 || c->f16 || c->tb || !c->tma ||
+      c->kernel != ST3D_KERNEL_TMA || c->tma->tj != 16 || c->tma->nv != 4 || !staged_ok(c))
+    return ST3D_OK;
+  const int pts = c->opts.points;
+  if (pts != 7 && pts != 13 && pts != 25) return ST3D_OK;
+  const size_t hbytes = host_array_bytes(c);
+  const float* hv = static_cast<const float*>(direct_view(v, hbytes));
+  const float* hs = static_cast<const float*>(direct_view(s, hbytes));
+  const float* hu = static_cast<const float*>(direct_view(u, hbytes));
+  if (!hv || !hs || !hu) return ST3D_OK;
+  int coop = 0, sm = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->device);
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, c->device);
+  const int per_sm = stream_blocks_per_sm(pts, c->opts.mode);
+  if (!coop || per_sm < 1) return ST3D_OK;
+
+  const st3d_grid_desc& gd = c->grid;
+  const bool wave = c->opts.mode == ST3D_MODE_WAVE;
+  const int R = c->R;
+  const int T = (int)iterations;
+  StreamPlan p;
+  p.chunk = c->opts.ichunk > 0 ? c->opts.ichunk : 16;
+  if (p.chunk < R) p.chunk = R;
+  p.nchunks = (int)((gd.xs + p.chunk - 1) / p.chunk);
+  p.ntk = c->tma->ntk;
+  p.ntiles = c->tma->ntj * c->tma->ntk;
+  p.grid = sm * per_sm;
+  p.n_xfer = p.grid >= 64 ? 16 : p.grid / 4;
+  if (p.n_xfer < 1 || p.grid - p.n_xfer < 1) return ST3D_OK;
+  const int S = p.nchunks;
+  if ((uint64_t)T * S * p.ntiles > 0x7fffffffull || (uint64_t)T * S > 0x7fffffffull) return ST3D_OK;
+
+  // host tables: the stencil queue (step, chunk) in wavefront order (step t
+  // of chunk c at stage c + t + 1, steps in increasing order within a stage),
+  // the transfer queue (uploads chunk by chunk, each chunk's downloads behind
+  // the uploads its last step depends on), the plane copies each chunk's
+  // upload counts, and the source amplitude of every step
+  const int hx = gd.xh < 4 ? (int)gd.xh : 4, hy = gd.yh < 4 ? (int)gd.yh : 4;
+  std::vector<int2> pairs;
+  pairs.reserve((size_t)T * S);
+  for (long long d = 1; d <= (long long)S + T - 1; ++d)
+    for (int t = 0; t < T; ++t) {
+      const long long cc = d - 1 - t;
+      if (cc >= 0 && cc < S) pairs.push_back(make_int2(t, (int)cc));
+    }
+  std::vector<int4> xfer;
+  std::vector<int> up_need(S, 0);
+  const int lag = wave ? T + 1 : 2;  // uploads ahead of a chunk's downloads
+  auto downloads = [&](int ch) {
+    const int i0 = ch * p.chunk, i1 = std::min((int)gd.xs, i0 + p.chunk);
+    for (int f = wave ? 0 : 1; f < 2; ++f)
+      for (int i = i0; i < i1; ++i) xfer.push_back(make_int4(1, f, i, ch));
+  };
+  for (int d = 0; d < S; ++d) {
+    const int i0 = d * p.chunk - (d == 0 ? hx : 0);
+    const int i1 = std::min((int)gd.xs, (d + 1) * p.chunk) + (d == S - 1 ? hx : 0);
+    for (int f = 0; f < 3; ++f)
+      for (int i = i0; i < i1; ++i) xfer.push_back(make_int4(0, f, i, d));
+    up_need[d] = 3 * (i1 - i0);
+    if (d - lag >= 0) downloads(d - lag);
+  }
+  for (int ch = std::max(0, S - lag); ch < S; ++ch) downloads(ch);
+  std::vector<float> amps;
+  if (wave && c->opts.src_i >= 0) {
+    amps.resize(T);
+    for (int t = 0; t < T; ++t)
+      amps[t] = (float)st3d_ricker((double)t * c->opts.dt, c->opts.src_f, c->opts.src_t0);
+  }
+
+  // one device buffer: pairs | xfer | up_need | amps | counters
+  auto align16 = [](size_t x) { return (x + 15) / 16 * 16; };
+  const size_t o_pairs = 0;
+  const size_t o_xfer = align16(o_pairs + pairs.size() * sizeof(int2));
+  const size_t o_need = align16(o_xfer + xfer.size() * sizeof(int4));
+  const size_t o_amps = align16(o_need + up_need.size() * sizeof(int));
+  const size_t o_cnt = align16(o_amps + amps.size() * sizeof(float));
+  const size_t ncnt = (size_t)S + (size_t)T * S + 1 + 2;  // up_cnt, st_cnt, progress, heads
+  const size_t need = o_cnt + ncnt * sizeof(int);
+  if (need > c->stream_buf_bytes) {
+    if (c->stream_buf) {
+      cudaFree(c->stream_buf);
+      c->bytes -= c->stream_buf_bytes;
+    }
+    c->stream_buf = nullptr;
+    c->stream_buf_bytes = 0;
+    cudaError_t e = cudaMalloc(&c->stream_buf, need);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ST3D_ERR_NOMEM, "cudaMalloc of %zu bytes for the streamed call failed", need);
+    }
+    c->stream_buf_bytes = need;
+    c->bytes += need;
+  }
+  // the previous call's copies out of stream_host have finished: the call
+  // synchronised its stream
+  c->stream_host.assign(o_cnt, 0);
+  unsigned char* hb = c->stream_host.data();
+  memcpy(hb + o_pairs, pairs.data(), pairs.size() * sizeof(int2));
+  memcpy(hb + o_xfer, xfer.data(), xfer.size() * sizeof(int4));
+  memcpy(hb + o_need, up_need.data(), up_need.size() * sizeof(int));
+  if (!amps.empty()) memcpy(hb + o_amps, amps.data(), amps.size() * sizeof(float));
+  unsigned char* db = static_cast<unsigned char*>(c->stream_buf);
+  ST3D_CUDA(cudaMemcpyAsync(db, hb, o_cnt, cudaMemcpyHostToDevice, c->stream));
+  ST3D_CUDA(cudaMemsetAsync(db + o_cnt, 0, ncnt * sizeof(int), c->stream));
+
+  StreamLaunch L;
+  L.g = c->G;
+  L.R = ref_geom(gd);
+  L.cf = c->cf32;
+  for (int f = 0; f < 3; ++f) L.fld[f] = static_cast<float*>(c->fld[f]);
+  L.hin[0] = hu;
+  L.hin[1] = hv;
+  L.hin[2] = hs;
+  L.hout[0] = const_cast<float*>(hu);
+  L.hout[1] = const_cast<float*>(hv);
+  L.ub0 = c->ub;
+  L.vb0 = c->vb;
+  L.steps = T;
+  L.pairs = reinterpret_cast<const int2*>(db + o_pairs);
+  L.xfer = reinterpret_cast<const int4*>(db + o_xfer);
+  L.nxfer = (int)xfer.size();
+  L.up_need = reinterpret_cast<const int*>(db + o_need);
+  int* cnt = reinterpret_cast<int*>(db + o_cnt);
+  L.up_cnt = cnt;
+  L.st_cnt = cnt + S;
+  L.progress = cnt + S + (size_t)T * S;
+  L.heads = L.progress + 1;
+  L.hx = hx;
+  L.hy = hy;
+  L.hz = (int)gd.zh;
+  const RefGeom& Rg = L.R;
+  const bool aligned = (reinterpret_cast<uintptr_t>(hu) | reinterpret_cast<uintptr_t>(hv) |
+                        reinterpret_cast<uintptr_t>(hs)) % 16 == 0;
+  L.vec = aligned && Rg.jmult % 4 == 0 && gd.zh % 4 == 0 && gd.zs % 4 == 0 &&
+          (c->L.pk - gd.zh) % 4 == 0;
+  L.src_i = wave ? c->opts.src_i : -1;
+  L.src_j = c->opts.src_j;
+  L.src_k = c->opts.src_k;
+  L.amps = amps.empty() ? nullptr : reinterpret_cast<const float*>(db + o_amps);
+  L.timeout_ns = c->tma->timeout_ns;
+  // any wait's cap: the timeout plus four times the call at 100 Gpts/s and
+  // the transfers at 20 GB/s, far beyond any run that makes progress
+  const double pts_all = (double)gd.xs * gd.ys * gd.zs;
+  L.cap_ns = L.timeout_ns + (uint64_t)(4.0 * (pts_all * T / 100.0 + 5.0 * hbytes / 20.0));
+  L.status = c->dev_status;
+  const CUtensorMap maps[5] = {c->tma->umap[0], c->tma->umap[1], c->tma->vmap[0], c->tma->vmap[1],
+                               c->tma->vmap[2]};
+  cudaError_t e = launch_stream(pts, c->opts.mode, p, maps, L, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "streamed call launch");
+  // the state a phase-by-phase call leaves: the source clock restarts at the
+  // upload and advances T steps; mode W swaps the pair every step
+  c->has_u = c->has_v = c->has_s = true;
+  c->pair_valid = false;
+  c->step = (uint64_t)T;
+  c->lvl += (uint64_t)T;
+  c->launches += 1;
+  if (wave && (T & 1)) {
+    const int t = c->ub;
+    c->ub = c->vb;
+    c->vb = t;
+  }
+  c->host_path = ST3D_HOST_STREAMED;
+  *done = true;
+  return ST3D_OK;
+}
+
 int check_device_status(st3d_ctx* c) {
   uint32_t st = 0;
   ST3D_CUDA(cudaMemcpyAsync(&st, c->dev_status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
@@ -1159,6 +1334,7 @@ int st3d_destroy(st3d_ctx* c) {
   if (c->counter) cudaFree(c->counter);
   if (c->dev_status) cudaFree(c->dev_status);
   if (c->stage) cudaFree(c->stage);
+  if (c->stream_buf) cudaFree(c->stream_buf);
   for (int f = 0; f < 2; ++f)
     if (c->lo[f]) cudaFree(c->lo[f]);
   if (c->E) cudaFree(c->E);
@@ -1452,7 +1628,11 @@ int st3d_inject_device_status(st3d_ctx* c, uint32_t code) {
 int st3d_iterate_host(st3d_ctx* c, void* v, const void* s, void* u, uint32_t iterations) {
   if (!c || !v || !s || !u) return fail(ST3D_ERR_INVALID, "null argument");
   DeviceScope scope(c->device);
-  int rc = st3d_upload(c, v, s, u);
+  bool streamed = false;
+  int rc = iterate_host_streamed(c, v, s, u, iterations, &streamed);
+  if (rc != ST3D_OK) return rc;
+  if (streamed) return st3d_synchronize(c);
+  rc = st3d_upload(c, v, s, u);
   if (rc == ST3D_OK) rc = st3d_iterate(c, iterations);
   if (rc == ST3D_OK)
     rc = st3d_download(c, v, c->opts.mode == ST3D_MODE_WAVE ? u : nullptr);

@@ -3,6 +3,8 @@
 // (st3d_batch.cu).
 #pragma once
 
+#include <vector>
+
 #include "st3d_internal.h"
 #include "st3d_tma.cuh"
 
@@ -69,4 +71,9 @@ struct st3d_ctx {
   Coefs<float> cf32;
   Coefs<double> cf64;
   size_t bytes = 0;
+  // the streamed drop-in call (st3d_stream.cu): its queues, counters and
+  // amplitudes on the device, and their host copies (kept until the next call)
+  void* stream_buf = nullptr;
+  size_t stream_buf_bytes = 0;
+  std::vector<unsigned char> stream_host;
 };

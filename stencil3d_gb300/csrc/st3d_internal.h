@@ -12,6 +12,7 @@
 // upload; the rest of the padding is zero.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -129,6 +130,38 @@ struct Source {
   float amp;     // s is replaced by s + amp at the source point
   double amp_d;  // the same amplitude for double storage
 };
+
+// The streamed drop-in call (st3d_stream.cu): host transfers and time steps
+// in one cooperative launch.  chunk: planes per chunk along i; n_xfer: CTAs
+// that copy planes between the host arrays and the device layout.
+struct StreamPlan {
+  int chunk = 16, nchunks = 0;
+  int ntk = 0, ntiles = 0;  // tiles per plane along k, tiles per plane
+  int n_xfer = 16, grid = 0;
+};
+struct StreamLaunch {
+  Geom g;
+  RefGeom R;
+  Coefs<float> cf;
+  float* fld[3];
+  const float* hin[3];  // device views of the host u, v, s
+  float* hout[2];       // device views of the host u, v written back
+  int ub0, vb0, steps;
+  const int2* pairs;
+  const int4* xfer;
+  int nxfer;
+  const int* up_need;
+  int *up_cnt, *st_cnt, *progress, *heads;
+  int hx, hy, hz, vec;
+  int src_i, src_j, src_k;
+  const float* amps;
+  uint64_t timeout_ns;  // a wait gives up after this long without progress anywhere
+  uint64_t cap_ns;      // and after this long in all
+  uint32_t* status;
+};
+int stream_blocks_per_sm(int points, int mode);
+cudaError_t launch_stream(int points, int mode, const StreamPlan& p, const CUtensorMap* maps,
+                          const StreamLaunch& L, cudaStream_t stream);
 
 // Device status word values set by bounded waits.
 enum DeviceStatus : uint32_t {
