@@ -17,6 +17,10 @@ if REPO not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 GPU (run with -m gpu)")
+    # the reference's own host path (oracle/_ref) before collection: test
+    # modules decide at import whether the live reference is there
+    from oracle import build as obuild
+    obuild.build_ref()
 
 
 # Where the reference's sources sit on the machine that built this checkout
@@ -29,11 +33,9 @@ if "ST3D_REFERENCE_DIR" not in os.environ and os.path.isfile(
 
 @pytest.fixture(scope="session", autouse=True)
 def _native_builds():
-    """Build libst3d.so, the oracle and, where its sources are given, the
-    reference's own host path (oracle/_ref) in-tree if missing or stale."""
+    """Build libst3d.so and the oracle in-tree if they are missing or stale."""
     from stencil3d_gb300 import build as pbuild
     from oracle import build as obuild
     pbuild.build()
     obuild.build_oracle()
-    obuild.build_ref()
     yield
