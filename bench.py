@@ -498,6 +498,7 @@ def e2e_run(S, st, g, calls, iters):
             st.timer_start()
             st.iterate_host(pv.array, ps.array, pu.array, iters)
             times.append(st.timer_stop())
+        path = st.info().host_path  # of the timed calls
         # the same call split into its phases, for the record
         phases = {}
         st.timer_start()
@@ -523,7 +524,7 @@ def e2e_run(S, st, g, calls, iters):
     return {"value": pts * iters / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "host_path": {0: "auto", 1: "staged", 2: "direct", 3: "strided",
-                          4: "streamed"}[st.info().host_path],
+                          4: "streamed"}[path],
             "step": "one ITERATE-equivalent call (st3d_iterate_host) of %d time steps" % iters,
             "ms_per_call": ms, "phases": phases,
             "h2d_gbs": h2d / (phases["upload_ms"] * 1e-3) / 1e9,

@@ -817,16 +817,18 @@ int iterate_host_streamed(st3d_ctx* c, void* v, const void* s, void* u, uint32_t
   p.ntk = c->tma->ntk;
   p.ntiles = c->tma->ntj * c->tma->ntk;
   p.grid = sm * per_sm;
-  p.n_xfer = p.grid >= 64 ? 16 : p.grid / 4;
-  if (p.n_xfer < 1 || p.grid - p.n_xfer < 1) return ST3D_OK;
+  if (p.grid < 64) {
+    p.n_up = p.n_down = p.grid / 8 > 0 ? p.grid / 8 : 1;
+  }
+  if (p.grid - p.n_up - p.n_down < 1) return ST3D_OK;
   const int S = p.nchunks;
   if ((uint64_t)T * S * p.ntiles > 0x7fffffffull || (uint64_t)T * S > 0x7fffffffull) return ST3D_OK;
 
   // host tables: the stencil queue (step, chunk) in wavefront order (step t
   // of chunk c at stage c + t + 1, steps in increasing order within a stage),
-  // the transfer queue (uploads chunk by chunk, each chunk's downloads behind
-  // the uploads its last step depends on), the plane copies each chunk's
-  // upload counts, and the source amplitude of every step
+  // the upload queue (chunk by chunk) followed by the download queue (chunk
+  // by chunk), the plane copies each chunk's upload counts, and the source
+  // amplitude of every step
   const int hx = gd.xh < 4 ? (int)gd.xh : 4, hy = gd.yh < 4 ? (int)gd.yh : 4;
   std::vector<int2> pairs;
   pairs.reserve((size_t)T * S);
@@ -837,21 +839,19 @@ int iterate_host_streamed(st3d_ctx* c, void* v, const void* s, void* u, uint32_t
     }
   std::vector<int4> xfer;
   std::vector<int> up_need(S, 0);
-  const int lag = wave ? T + 1 : 2;  // uploads ahead of a chunk's downloads
-  auto downloads = [&](int ch) {
-    const int i0 = ch * p.chunk, i1 = std::min((int)gd.xs, i0 + p.chunk);
-    for (int f = wave ? 0 : 1; f < 2; ++f)
-      for (int i = i0; i < i1; ++i) xfer.push_back(make_int4(1, f, i, ch));
-  };
   for (int d = 0; d < S; ++d) {
     const int i0 = d * p.chunk - (d == 0 ? hx : 0);
     const int i1 = std::min((int)gd.xs, (d + 1) * p.chunk) + (d == S - 1 ? hx : 0);
     for (int f = 0; f < 3; ++f)
       for (int i = i0; i < i1; ++i) xfer.push_back(make_int4(0, f, i, d));
     up_need[d] = 3 * (i1 - i0);
-    if (d - lag >= 0) downloads(d - lag);
   }
-  for (int ch = std::max(0, S - lag); ch < S; ++ch) downloads(ch);
+  const int nup = (int)xfer.size();
+  for (int ch = 0; ch < S; ++ch) {
+    const int i0 = ch * p.chunk, i1 = std::min((int)gd.xs, i0 + p.chunk);
+    for (int f = wave ? 0 : 1; f < 2; ++f)
+      for (int i = i0; i < i1; ++i) xfer.push_back(make_int4(1, f, i, ch));
+  }
   std::vector<float> amps;
   if (wave && c->opts.src_i >= 0) {
     amps.resize(T);
@@ -866,7 +866,7 @@ int iterate_host_streamed(st3d_ctx* c, void* v, const void* s, void* u, uint32_t
   const size_t o_need = align16(o_xfer + xfer.size() * sizeof(int4));
   const size_t o_amps = align16(o_need + up_need.size() * sizeof(int));
   const size_t o_cnt = align16(o_amps + amps.size() * sizeof(float));
-  const size_t ncnt = (size_t)S + (size_t)T * S + 1 + 2;  // up_cnt, st_cnt, progress, heads
+  const size_t ncnt = (size_t)S + (size_t)T * S + 1 + 3;  // up_cnt, st_cnt, progress, heads
   const size_t need = o_cnt + ncnt * sizeof(int);
   if (need > c->stream_buf_bytes) {
     if (c->stream_buf) {
@@ -910,6 +910,7 @@ int iterate_host_streamed(st3d_ctx* c, void* v, const void* s, void* u, uint32_t
   L.steps = T;
   L.pairs = reinterpret_cast<const int2*>(db + o_pairs);
   L.xfer = reinterpret_cast<const int4*>(db + o_xfer);
+  L.nup = nup;
   L.nxfer = (int)xfer.size();
   L.up_need = reinterpret_cast<const int*>(db + o_need);
   int* cnt = reinterpret_cast<int*>(db + o_cnt);

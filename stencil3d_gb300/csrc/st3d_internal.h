@@ -132,12 +132,12 @@ struct Source {
 };
 
 // The streamed drop-in call (st3d_stream.cu): host transfers and time steps
-// in one cooperative launch.  chunk: planes per chunk along i; n_xfer: CTAs
-// that copy planes between the host arrays and the device layout.
+// in one cooperative launch.  chunk: planes per chunk along i; n_up, n_down:
+// CTAs that copy planes from the host arrays into the device layout and back.
 struct StreamPlan {
   int chunk = 16, nchunks = 0;
   int ntk = 0, ntiles = 0;  // tiles per plane along k, tiles per plane
-  int n_xfer = 16, grid = 0;
+  int n_up = 12, n_down = 12, grid = 0;
 };
 struct StreamLaunch {
   Geom g;
@@ -148,8 +148,8 @@ struct StreamLaunch {
   float* hout[2];       // device views of the host u, v written back
   int ub0, vb0, steps;
   const int2* pairs;
-  const int4* xfer;
-  int nxfer;
+  const int4* xfer;  // uploads [0, nup), downloads [nup, nxfer)
+  int nup, nxfer;
   const int* up_need;
   int *up_cnt, *st_cnt, *progress, *heads;
   int hx, hy, hz, vec;

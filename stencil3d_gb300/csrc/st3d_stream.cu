@@ -10,12 +10,14 @@
 // previous step's planes within R of it.  So the streamed call cuts the grid
 // into chunks of C planes along i and runs, in ONE launch:
 //
-//   - transfer CTAs (the first `n_xfer` CTAs, all warps copying): a queue of
+//   - upload CTAs (the first `n_up` CTAs, all warps copying): a queue of
 //     plane copies in chunk order -- every plane of u, v and s of chunk d
 //     from the pinned host array into the device layout (the host array's
-//     device view; halo planes with the first and last chunk), then publish
-//     the chunk's upload count; the download of a chunk's final v (and u)
-//     planes sits in the queue behind the uploads its last step depends on;
+//     device view; halo planes with the first and last chunk), each counted
+//     in the chunk's upload counter;
+//   - download CTAs (the next `n_down`): a queue of the final v (and u)
+//     planes in chunk order, each copied out once the last step of its chunk
+//     has finished (their waits never hold up an upload);
 //   - stencil CTAs (the rest; the k_tma kernel's producer/consumer structure,
 //     16-row x 128-point tiles, 4 stages): a queue of (step t, chunk c, tile)
 //     items in wavefront order -- step t of chunk c is queued at stage
@@ -70,14 +72,14 @@ struct StreamArgs {
   int ntk, ntiles;      // tiles per plane along k, tiles per plane
   const int2* pairs;    // (step, chunk) in wavefront order
   int npairs;
-  const int4* xfer;     // (kind, field, plane, chunk) in queue order
-  int nxfer;
+  const int4* xfer;     // (kind, field, plane, chunk): uploads [0, nup), downloads [nup, nxfer)
+  int nup, nxfer;
   const int* up_need;   // per chunk: plane copies to upload
   int* up_cnt;          // per chunk: plane copies uploaded
   int* st_cnt;          // per (step, chunk): tiles finished
   int* progress;        // tiles + plane copies finished (liveness of the waits)
-  int* heads;           // [0] stencil queue, [1] transfer queue
-  int n_xfer;           // transfer CTAs
+  int* heads;           // [0] stencil queue, [1] upload queue, [2] download queue
+  int n_up, n_down;     // upload and download CTAs
   int hx, hy, hz;       // halo widths moved
   int vec;              // rows move as float4 (16-byte aligned on both sides)
   int src_i, src_j, src_k;
@@ -232,14 +234,17 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
 
-  if ((int)blockIdx.x < a.n_xfer) {
+  if ((int)blockIdx.x < a.n_up + a.n_down) {
     // ---------------- transfer CTA ----------------
     int* s_item = reinterpret_cast<int*>(smem_raw);  // kind, field, plane, chunk, stop
     const int last_step = a.steps - 1;
+    const bool up = (int)blockIdx.x < a.n_up;
+    int* head = a.heads + (up ? 1 : 2);
+    const int first = up ? 0 : a.nup, end = up ? a.nup : a.nxfer;
     while (true) {
       if (threadIdx.x == 0) {
-        const int x = atomicAdd(&a.heads[1], 1);
-        int stop = x >= a.nxfer;
+        const int x = first + atomicAdd(head, 1);
+        int stop = x >= end;
         int4 it = make_int4(0, 0, 0, 0);
         if (!stop) {
           it = a.xfer[x];
@@ -592,13 +597,15 @@ cudaError_t launch_stream(int points, int mode, const StreamPlan& p, const CUten
   a.pairs = L.pairs;
   a.npairs = L.steps * p.nchunks;
   a.xfer = L.xfer;
+  a.nup = L.nup;
   a.nxfer = L.nxfer;
   a.up_need = L.up_need;
   a.up_cnt = L.up_cnt;
   a.st_cnt = L.st_cnt;
   a.progress = L.progress;
   a.heads = L.heads;
-  a.n_xfer = p.n_xfer;
+  a.n_up = p.n_up;
+  a.n_down = p.n_down;
   a.hx = L.hx;
   a.hy = L.hy;
   a.hz = L.hz;
