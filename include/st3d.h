@@ -244,7 +244,9 @@ int st3d_download(st3d_ctx* ctx, void* v, void* u);
 int st3d_iterate(st3d_ctx* ctx, uint32_t iterations);
 /* ITERATE drop-in on host arrays: upload v, s, u; iterate; download v (and,
  * in mode W, u as well: u is then written although ITERATE declares it
- * const); synchronize. */
+ * const); synchronize.  With pinned arrays on an FP32 TMA context (host path
+ * AUTO or STREAMED) the three phases overlap in one launch (see
+ * ST3D_HOST_STREAMED); the host arrays end the same either way. */
 int st3d_iterate_host(st3d_ctx* ctx, void* v, const void* s, void* u, uint32_t iterations);
 /* Waits for the context's stream; ST3D_ERR_TIMEOUT if a bounded device-side
  * wait of a kernel gave up since the last call (the kernel then returned

@@ -14,7 +14,8 @@
 //     plane copies in chunk order -- every plane of u, v and s of chunk d
 //     from the pinned host array into the device layout (the host array's
 //     device view; halo planes with the first and last chunk), each counted
-//     in the chunk's upload counter;
+//     in the chunk's upload counter; once their queue is drained they join
+//     the stencil queue;
 //   - download CTAs (the next `n_down`): a queue of the final v (and u)
 //     planes in chunk order, each copied out once the last step of its chunk
 //     has finished (their waits never hold up an upload);
@@ -26,7 +27,8 @@
 //     else every tile of step t-1 of chunks c-1..c+1 (mode W: step t reads
 //     U^t of its halo planes and overwrites U^{t-1}, which step t-1 read with
 //     its halo) or of chunk c alone (mode R: u and s are fixed, v is updated
-//     in place without a halo).
+//     in place without a halo).  A producer skips the check for the next
+//     tile of the (step, chunk) whose inputs it saw complete.
 //
 // Every dependency is on an item earlier in its own queue or in the other
 // queue's order, and the cooperative launch keeps all CTAs resident, so
@@ -233,6 +235,23 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
   const Geom& g = a.g;
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
+  float* ur = reinterpret_cast<float*>(smem_raw);
+  float* vr = ur + NU * USLOT;
+  float* sr = vr + NV * VSLOT;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sr + NV * VSLOT);
+  uint64_t* empty = full + NV;
+  SStage* info = reinterpret_cast<SStage*>(empty + NV);
+  unsigned* finished = reinterpret_cast<unsigned*>(info + NV);
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < kSlots; ++q) finished[q] = 0u;
+    for (int s = 0; s < NV; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], TJ);
+    }
+    fence_barrier_init();
+    fence_proxy_async_smem();
+  }
+  __syncthreads();
 
   if ((int)blockIdx.x < a.n_up + a.n_down) {
     // ---------------- transfer CTA ----------------
@@ -252,7 +271,7 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
               !wait_live(a.st_cnt + (size_t)last_step * a.nchunks + it.w, a.ntiles, a.progress,
                          a.timeout_ns, a.cap_ns)) {
             atomicExch(a.status, (uint32_t)kDevTimeoutDep);
-            stop = 1;
+            stop = 2;
           }
         }
         s_item[0] = it.x;
@@ -284,29 +303,15 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
       // s_item is rewritten only after the next loop's first barrier
       __syncthreads();
     }
-    return;
+    // An upload CTA whose queue is drained joins the stencil queue (the
+    // steps are what is left to do); s_item, which lies in the u ring, is no
+    // longer read once every thread has passed this barrier.
+    __syncthreads();
+    if (!up || s_item[4] == 2) return;
+    __syncthreads();
   }
 
   // ---------------- stencil CTA ----------------
-  float* ur = reinterpret_cast<float*>(smem_raw);
-  float* vr = ur + NU * USLOT;
-  float* sr = vr + NV * VSLOT;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sr + NV * VSLOT);
-  uint64_t* empty = full + NV;
-  SStage* info = reinterpret_cast<SStage*>(empty + NV);
-  unsigned* finished = reinterpret_cast<unsigned*>(info + NV);
-
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < kSlots; ++q) finished[q] = 0u;
-    for (int s = 0; s < NV; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], TJ);
-    }
-    fence_barrier_init();
-    fence_proxy_async_smem();
-  }
-  __syncthreads();
-
   const int total = a.npairs * a.ntiles;
   if (warp == TJ) {
     // ---------------- producer ----------------
@@ -318,6 +323,7 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
     tma_prefetch_desc(&smap);
     uint32_t h = 0;
     bool ok = true;
+    int dep_t = -1, dep_c = -1;  // the (step, chunk) whose inputs were seen complete
     while (ok) {
       const int x = atomicAdd(&a.heads[0], 1);
       if (x >= total) {
@@ -335,20 +341,35 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
       const int tile = x - pi * a.ntiles;
       const int2 tc = a.pairs[pi];
       const int t = tc.x, c = tc.y;
-      // inputs of step t of chunk c
       const bool wave = MODE == ST3D_MODE_WAVE;
-      for (int cc = c - 1; cc <= c + 1 && ok; ++cc) {
-        if (cc < 0 || cc >= a.nchunks) continue;
-        if (t == 0) {
-          ok = wait_live(a.up_cnt + cc, a.up_need[cc], a.progress, a.timeout_ns, a.cap_ns);
-        } else if (wave || cc == c) {
-          ok = wait_live(a.st_cnt + (size_t)(t - 1) * a.nchunks + cc, a.ntiles, a.progress,
-                         a.timeout_ns, a.cap_ns);
+      if (t != dep_t || c != dep_c) {
+        // inputs of step t of chunk c: one pass of loads, then waits on the
+        // counters not yet complete; consecutive tiles of one (step, chunk)
+        // skip it
+        const int* ctr[3];
+        int target[3];
+        bool done[3];
+        for (int q = 0; q < 3; ++q) {
+          const int cc = c - 1 + q;
+          ctr[q] = nullptr;
+          if (cc < 0 || cc >= a.nchunks) continue;
+          if (t == 0) {
+            ctr[q] = a.up_cnt + cc;
+            target[q] = a.up_need[cc];
+          } else if (wave || cc == c) {
+            ctr[q] = a.st_cnt + (size_t)(t - 1) * a.nchunks + cc;
+            target[q] = a.ntiles;
+          }
         }
-      }
-      if (!ok) {
-        atomicExch(a.status, (uint32_t)kDevTimeoutDep);
-        break;
+        for (int q = 0; q < 3; ++q) done[q] = !ctr[q] || ld_acquire(ctr[q]) >= target[q];
+        for (int q = 0; q < 3 && ok; ++q)
+          if (!done[q]) ok = wait_live(ctr[q], target[q], a.progress, a.timeout_ns, a.cap_ns);
+        if (!ok) {
+          atomicExch(a.status, (uint32_t)kDevTimeoutDep);
+          break;
+        }
+        dep_t = t;
+        dep_c = c;
       }
       proxy_fence_global();
       const int ub = wave ? (a.ub0 ^ (t & 1)) : a.ub0;
