@@ -382,7 +382,9 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
       const int ia = c * a.chunk;
       const int ib = min(ia + a.chunk, g.xs);
       const int nsteps = (ib - ia) + 2 * R;
-      for (int n = 0; n < nsteps; ++n, ++h) {
+      // the first R planes of the unit enter the consumers' queues by direct
+      // loads: no pipeline step for them
+      for (int n = R; n < nsteps; ++n, ++h) {
         const int stage = (int)(h % NV);
         if (h >= (uint32_t)NV &&
             !mbar_wait_bounded(&empty[stage], ((h / NV) - 1) & 1u, a.timeout_ns)) {
@@ -440,7 +442,27 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
       for (int ph = 0; ph < QN; ++ph) {
         const int n = n0 + ph;
         if (n >= nsteps) break;
-        const uint32_t hh = h + (uint32_t)n;
+        if (n < R) {
+          // a queue plane below the unit (u plane ia - R + n): read straight
+          // from the field, after the item's first stage completed (its
+          // inputs are then visible); where the TMA tile would be out of the
+          // tensor map's extent (rows >= ys + 4, columns >= zs + 4) it is zero
+          const int p = ia - R + n;
+          const float* src = a.fld[ub] + g.org + (long long)p * g.si + (long long)j * g.sj + k;
+          float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (j < g.ys + 4) {
+            if (k + 3 < g.zs + 4) {
+              x4 = __ldcg(reinterpret_cast<const float4*>(src));
+            } else {
+              if (k < g.zs + 4) x4.x = __ldcg(src);
+              if (k + 1 < g.zs + 4) x4.y = __ldcg(src + 1);
+              if (k + 2 < g.zs + 4) x4.z = __ldcg(src + 2);
+            }
+          }
+          q[ph] = x4;
+          continue;
+        }
+        const uint32_t hh = h + (uint32_t)(n - R);
         const int stage = (int)(hh % NV);
         if (!mbar_wait_bounded(&full[stage], (hh / NV) & 1u, a.timeout_ns)) {
           atomicExch(a.status, (uint32_t)kDevTimeoutFull);
@@ -544,7 +566,7 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
       }
     }
     ++seq;
-    h += (uint32_t)nsteps;
+    h += (uint32_t)(nsteps - R);
   }
 }
 
