@@ -137,7 +137,7 @@ struct Source {
 struct StreamPlan {
   int chunk = 16, nchunks = 0;
   int ntk = 0, ntiles = 0;  // tiles per plane along k, tiles per plane
-  int n_up = 12, n_down = 12, grid = 0;
+  int n_up = 16, n_down = 12, grid = 0;
 };
 struct StreamLaunch {
   Geom g;

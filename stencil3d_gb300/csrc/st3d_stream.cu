@@ -105,6 +105,15 @@ __device__ __forceinline__ void red_release_add(int* p, int v) {
   asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ unsigned atom_add_acq_rel_cta(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "r"(static_cast<uint32_t>(__cvta_generic_to_shared(p))), "r"(v)
+               : "memory");
+  return old;
+}
+
 __device__ __forceinline__ void proxy_fence_global() {
   asm volatile("fence.proxy.async.global;" ::: "memory");
 }
@@ -552,14 +561,15 @@ __global__ void __launch_bounds__((kSTJ + 1) * 32, 1)
     // the tile is stored by this warp; the CTA's last warp to finish it
     // publishes it (a warp runs at most NV stages, so at most NV items,
     // ahead of the slowest: 2 NV counters never mix two items)
+    // (The warp's stores are ordered before lane 0's release on the CTA
+    // counter by __syncwarp; the last warp's acquire on it orders every
+    // warp's stores before its gpu-scope release, which is cumulative.)
     __syncwarp();
     if (lane == 0) {
       unsigned* slot = finished + (seq % kSlots);
-      __threadfence();
-      const unsigned old = atomicAdd(slot, 1u);
+      const unsigned old = atom_add_acq_rel_cta(slot, 1u);
       if (old == TJ - 1) {
         atomicExch(slot, 0u);
-        __threadfence();
         proxy_fence_global();
         red_release_add(a.st_cnt + (size_t)t * a.nchunks + c, 1);
         red_release_add(a.progress, 1);
