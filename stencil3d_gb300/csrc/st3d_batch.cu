@@ -616,10 +616,12 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
     o.tile_j = 16;  // the single-grid plan, used by the sequential schedule
     o.stages = 4;
     o.temporal_block = 1;  // the batch steps one level at a time
-    // planes per unit: 256 measured best on the 64-grid batch (graph 350.4
-    // against 341.6 Gpts/s with 64; pipelined 361.1 against 338.0): fewer
-    // units re-read fewer warm-up planes and the queue still balances
-    if (o.ichunk <= 0) o.ichunk = 256;
+    // Planes per unit of the batch kernel: 256 measured best on the 64-grid
+    // batch (graph 350.4 against 341.6 Gpts/s with 64; pipelined 361.1
+    // against 338.0): fewer units re-read fewer warm-up planes and the shared
+    // queue still balances.  The grid's own context keeps the single-grid
+    // planner's choice (opts.ichunk 0), which the sequential schedule runs.
+    const int batch_ichunk = o.ichunk > 0 ? o.ichunk : 256;
     st3d_ctx* c = nullptr;
     rc = create_context(&grids[gi], &o, b->stream, &c);
     if (rc != ST3D_OK) return cleanup(rc);
@@ -637,7 +639,7 @@ int st3d_batch_create(uint32_t n, const st3d_grid_desc* grids, const st3d_opts* 
     const long long wide = (ys + kBTJ - 1) / kBTJ * kBTJ * ((zs + kTmaTK - 1) / kTmaTK * kTmaTK);
     const long long thin = (ys + kNTJ - 1) / kNTJ * kNTJ * ((zs + kNTK - 1) / kNTK * kNTK);
     G.narrow = thin < wide ? 1 : 0;
-    G.ichunk = c->tma->ichunk;
+    G.ichunk = batch_ichunk;
     const int tk = G.narrow ? kNTK : kTmaTK, tj = G.narrow ? kNTJ : kBTJ;
     G.ntk = (int)((zs + tk - 1) / tk);
     G.ntjk = (int)((ys + tj - 1) / tj) * G.ntk;
