@@ -85,7 +85,12 @@ typedef enum st3d_storage {
 typedef enum st3d_kernel {
   ST3D_KERNEL_AUTO = 0,   /* the fastest kernel for the request */
   ST3D_KERNEL_SIMPLE = 1, /* direct-load 2.5D streaming kernel (all storages) */
-  ST3D_KERNEL_TMA = 2     /* TMA-staged 2.5D streaming kernel (F32 and the 16-bit storages) */
+  ST3D_KERNEL_TMA = 2,    /* TMA-staged 2.5D streaming kernel (F32 and the 16-bit storages) */
+  /* The 16-bit delta forms (F16, BF16, F16_HL) with the j and k neighbour
+   * sums as band-matrix products on the tensor cores (FP32 accumulation):
+   * the same update, within FP32 rounding of the sum per step, not bit for
+   * bit the TMA kernel's result. */
+  ST3D_KERNEL_MMA = 3
 } st3d_kernel;
 
 typedef enum st3d_field {

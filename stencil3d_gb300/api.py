@@ -20,14 +20,14 @@ LIB_PATH = os.path.join(_HERE, "_build", "libst3d.so")
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_STATE, ERR_NODEVICE = range(8)
 MODE_REF, MODE_WAVE = 0, 1
 F32, F64, F16, BF16, F16_HILO, F16_HL = 0, 1, 2, 3, 4, 5
-KERNEL_AUTO, KERNEL_SIMPLE, KERNEL_TMA = 0, 1, 2
+KERNEL_AUTO, KERNEL_SIMPLE, KERNEL_TMA, KERNEL_MMA = 0, 1, 2, 3
 FIELD_U, FIELD_V, FIELD_S = 0, 1, 2
 FILL_CONST, FILL_UNIFORM, FILL_BLOBS = 0, 1, 2
 HOST_AUTO, HOST_STAGED, HOST_DIRECT, HOST_STRIDED, HOST_STREAMED = 0, 1, 2, 3, 4
 
 _MODES = {"ref": MODE_REF, "wave": MODE_WAVE}
 _STORAGES = {"f32": F32, "f64": F64, "f16": F16, "bf16": BF16, "f16_hilo": F16_HILO, "f16_hl": F16_HL}
-_KERNELS = {"auto": KERNEL_AUTO, "simple": KERNEL_SIMPLE, "tma": KERNEL_TMA}
+_KERNELS = {"auto": KERNEL_AUTO, "simple": KERNEL_SIMPLE, "tma": KERNEL_TMA, "mma": KERNEL_MMA}
 
 
 class St3dError(RuntimeError):

@@ -29,7 +29,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false",
                      "-I", os.path.join(REPO, "include"), "-I", CSRC]
 
 CU_SOURCES = ["st3d_api.cu", "st3d_kernels_simple.cu", "st3d_kernels_tma.cu",
-              "st3d_kernels_tma16.cu", "st3d_kernels_delta16.cu", "st3d_kernels_tb.cu",
+              "st3d_kernels_tma16.cu", "st3d_kernels_delta16.cu", "st3d_kernels_mma16.cu",
+              "st3d_kernels_tb.cu",
               "st3d_kernels_aux.cu", "st3d_kernels_copy.cu", "st3d_noalloc.cu", "st3d_batch.cu",
               "st3d_stream.cu"]
 

@@ -144,7 +144,7 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
   if (o->mode != ST3D_MODE_REF && o->mode != ST3D_MODE_WAVE)
     return fail(ST3D_ERR_INVALID, "unknown mode %d", o->mode);
   if (elem_bytes(o->storage) == 0) return fail(ST3D_ERR_INVALID, "unknown storage %d", o->storage);
-  if (o->kernel < ST3D_KERNEL_AUTO || o->kernel > ST3D_KERNEL_TMA)
+  if (o->kernel < ST3D_KERNEL_AUTO || o->kernel > ST3D_KERNEL_MMA)
     return fail(ST3D_ERR_INVALID, "unknown kernel %d", o->kernel);
   const int grc = st3d::validate_grid_limits(g);
   if (grc != ST3D_OK) return grc;
@@ -164,6 +164,13 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage runs on the TMA kernel only");
   if (s16 && (g->xs > 65535 - 8 || g->ys > 65535 - 8 || g->zh > 64))
     return fail(ST3D_ERR_UNSUPPORTED, "16-bit storage needs xs, ys <= 65527 and zh <= 64");
+  const bool delta16 = o->storage == ST3D_F16 || o->storage == ST3D_BF16 || o->storage == ST3D_F16_HL;
+  if (o->kernel == ST3D_KERNEL_MMA && !delta16)
+    return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel serves the 16-bit delta forms (F16, BF16, F16_HL)");
+  if (o->kernel == ST3D_KERNEL_MMA && o->tile_j != 0 && o->tile_j != 16)
+    return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel runs 16-row tiles, not %d", o->tile_j);
+  if (o->kernel == ST3D_KERNEL_MMA && o->stages != 0 && o->stages != 8)
+    return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel runs 8 stages, not %d", o->stages);
   if (o->kernel == ST3D_KERNEL_TMA && o->storage == ST3D_F64)
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves FP32 and 16-bit storage");
   if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
@@ -562,6 +569,65 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
   if (ok == ST3D_OK) ok = encode_map_t(&p->vhi[2], w16, 2, c->fld[2], c->L, 128, p->tj, 0, 0);
   if (ok == ST3D_OK && c->delta) ok = encode_map_t(&p->dmap, w16, 2, c->fld[3], c->L, 128, p->tj, 0, 0);
   if (ok != ST3D_OK) {
+    delete p;
+    return ok;
+  }
+  c->tma16 = p;
+  return ST3D_OK;
+}
+
+// Tensor-core delta-form plan (st3d_kernels_mma16.cu): 16-row x 120-column
+// tiles; tensor maps with a u box of 136 x 24 words (columns k0-8 .., rows
+// j0-R ..), d / s / lo boxes of 120 x 16 words, and interior boxes of 120 x
+// 16 over the u buffers for the stores of u^{n+1}.
+int plan_mma16(st3d_ctx* c, int sm_count, int max_smem) {
+  Tma16Plan* p = new (std::nothrow) Tma16Plan();
+  if (!p) return fail(ST3D_ERR_NOMEM, "host allocation failed");
+  const int R = c->R;
+  p->radius = R;
+  p->tj = 16;
+  p->delta = true;
+  p->pair = c->pair;
+  p->mma = true;
+  p->nb = 1;
+  p->nv = 8;
+  p->smem = mma16_smem_bytes(p->nv, R, c->pair);
+  const int per_sm =
+      (int)p->smem <= max_smem ? mma16_blocks_per_sm(c->opts.storage, c->opts.points, *p) : 0;
+  if (per_sm < 1) {
+    delete p;
+    return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel does not fit in shared memory");
+  }
+  if (cudaMalloc(&p->mma_rec, (size_t)c->L.xs * sizeof(MmaRecord)) != cudaSuccess) {
+    cudaGetLastError();
+    delete p;
+    return fail(ST3D_ERR_NOMEM, "cudaMalloc of the plane records failed");
+  }
+  c->bytes += (size_t)c->L.xs * sizeof(MmaRecord);
+  p->ntj = (int)((c->L.ys + 15) / 16);
+  p->ntk = (int)((c->L.zs + kMmaTK - 1) / kMmaTK);
+  const int ctas = sm_count * per_sm;
+  p->ichunk = c->opts.ichunk > 0 ? c->opts.ichunk : tma_pick_ichunk((int)c->L.xs, p->ntj * p->ntk, ctas, R);
+  p->nti = (int)((c->L.xs + p->ichunk - 1) / p->ichunk);
+  p->units = p->ntj * p->ntk * p->nti;
+  p->grid = ctas < p->units ? ctas : p->units;
+  p->threads = 16 * 32;
+  const CUtensorMapDataType w16 =
+      c->opts.storage == ST3D_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+  int ok = ST3D_OK;
+  for (int f = 0; f < 2 && ok == ST3D_OK; ++f) {
+    ok = encode_map_t(&p->uhi[f], w16, 2, c->fld[f], c->L, kMmaTK + 16, 24, 8, c->L.pj);
+    // the interior box the kernel stores u^{n+1} through
+    if (ok == ST3D_OK) ok = encode_map_t(&p->vhi[f], w16, 2, c->fld[f], c->L, kMmaTK, 16, 0, 0);
+    if (ok == ST3D_OK && c->pair)
+      ok = encode_map_t(&p->lo[f], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, c->lo[f], c->L, kMmaTK, 16, 0, 0);
+    else if (ok == ST3D_OK)
+      p->lo[f] = p->uhi[f];  // unused without the pair form
+  }
+  if (ok == ST3D_OK) ok = encode_map_t(&p->vhi[2], w16, 2, c->fld[2], c->L, kMmaTK, 16, 0, 0);
+  if (ok == ST3D_OK) ok = encode_map_t(&p->dmap, w16, 2, c->fld[3], c->L, kMmaTK, 16, 0, 0);
+  if (ok != ST3D_OK) {
+    cudaFree(p->mma_rec);
     delete p;
     return ok;
   }
@@ -1145,6 +1211,11 @@ int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info
   info->kernel = tma ? ST3D_KERNEL_TMA : ST3D_KERNEL_SIMPLE;
   info->tile_j = tma ? tj : 0;
   info->tile_k = tma ? kTmaTK : 0;
+  if (delta && opts->kernel == ST3D_KERNEL_MMA) {
+    info->kernel = ST3D_KERNEL_MMA;
+    info->tile_j = 16;
+    info->tile_k = kMmaTK;
+  }
   info->ichunk = opts->ichunk > 0 ? opts->ichunk : (tma ? 128 : 64);
   info->temporal_block = opts->temporal_block > 0 ? opts->temporal_block : 1;
   info->device = opts->device;
@@ -1282,9 +1353,10 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
     c->m2s = (float)(-2.0 * sw);
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-    rc = plan_tma16(c, sm, max_smem);
+    const bool mma = c->delta && c->opts.kernel == ST3D_KERNEL_MMA;
+    rc = mma ? plan_mma16(c, sm, max_smem) : plan_tma16(c, sm, max_smem);
     if (rc != ST3D_OK) return cleanup(rc);
-    c->kernel = ST3D_KERNEL_TMA;
+    c->kernel = mma ? ST3D_KERNEL_MMA : ST3D_KERNEL_TMA;
   }
 
   // kernel choice
@@ -1341,6 +1413,7 @@ int st3d_destroy(st3d_ctx* c) {
   if (c->E) cudaFree(c->E);
   if (c->M) cudaFree(c->M);
   if (c->halo_max) cudaFree(c->halo_max);
+  if (c->tma16 && c->tma16->mma_rec) cudaFree(c->tma16->mma_rec);
   delete c->tma16;
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -1364,7 +1437,7 @@ int st3d_get_info(const st3d_ctx* c, st3d_info* info) {
   info->bytes_per_point = c->tb ? 20.0 / c->tb->T : f16_bytes(c->opts.storage, c->opts.points, c->eb);
   info->flops_per_point = c->opts.points == 2 ? 2 : c->opts.points == 7 ? 12 : c->opts.points == 13 ? 29 : 41;
   info->tile_j = c->tma ? c->tma->tj : c->tma16 ? c->tma16->tj : 0;
-  info->tile_k = (c->tma || c->tma16) ? kTmaTK : 0;
+  info->tile_k = (c->tma16 && c->tma16->mma) ? kMmaTK : (c->tma || c->tma16) ? kTmaTK : 0;
   info->ichunk = c->tma ? c->tma->ichunk : c->tma16 ? c->tma16->ichunk : c->ichunk;
   info->temporal_block = c->opts.temporal_block;
   info->host_path = c->host_path;
@@ -1566,8 +1639,10 @@ int st3d_iterate(st3d_ctx* c, uint32_t iterations) {
       st.m2s = c->m2s;
       st.ubuf = ub;
       st.lout = c->pair ? (uint16_t*)c->lo[un] : nullptr;
-      e = launch_delta16(c->opts.storage, c->opts.points, *c->tma16, c->G, c->cf32, st, src,
-                         c->dev_status, c->stream);
+      e = c->tma16->mma ? launch_mma16(c->opts.storage, c->opts.points, *c->tma16, c->G, c->cf32, st,
+                                       src, c->dev_status, c->stream)
+                        : launch_delta16(c->opts.storage, c->opts.points, *c->tma16, c->G, c->cf32, st,
+                                         src, c->dev_status, c->stream);
       c->pair_valid = false;
     } else if (c->f16) {
       const long long n = (long long)c->lvl;

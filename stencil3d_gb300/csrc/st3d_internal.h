@@ -233,6 +233,16 @@ int delta16_blocks_per_sm(int storage, int points, const Tma16Plan& pl);
 cudaError_t launch_delta16(int storage, int points, const Tma16Plan& pl, const Geom& g,
                            const Coefs<float>& cf, const Delta16Step& st, const Source& src,
                            uint32_t* dev_status, cudaStream_t stream);
+// The plane-scale kernel run before each delta-form step (both kernels).
+cudaError_t launch_scales_delta(const Geom& g, int R, const Delta16Step& st, float c2, const Source& src,
+                                cudaStream_t stream);
+// The delta form with the j and k neighbour sums on the tensor cores
+// (st3d_kernels_mma16.cu); plan fields mma / nb.
+size_t mma16_smem_bytes(int nv, int R, bool pair);
+int mma16_blocks_per_sm(int storage, int points, const Tma16Plan& pl);
+cudaError_t launch_mma16(int storage, int points, const Tma16Plan& pl, const Geom& g,
+                         const Coefs<float>& cf, const Delta16Step& st, const Source& src,
+                         uint32_t* dev_status, cudaStream_t stream);
 size_t tma16_smem_bytes(int tj, int nv, int R, bool hilo);
 int tma16_blocks_per_sm(int storage, int points, const Tma16Plan& pl);
 cudaError_t launch_tma16(int storage, int points, const Tma16Plan& pl, const Geom& g,

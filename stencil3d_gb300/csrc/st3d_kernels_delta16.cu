@@ -554,12 +554,17 @@ cudaError_t launch_delta16(int storage, int points, const Tma16Plan& pl, const G
   a.lout = st.lout;
   if (pl.pair != (st.lout != nullptr)) return cudaErrorInvalidValue;
   const CUtensorMap maps[4] = {pl.uhi[st.ubuf], pl.dmap, pl.vhi[2], pl.lo[st.ubuf]};
-  k_scales_delta<<<(g.xs + 255) / 256, 256, 0, stream>>>(g.xs, pl.radius, st.Mu, st.Md, st.Ms,
-                                                         st.Eu_out, st.Ed_out, st.Mu_out, st.Md_out,
-                                                         st.k4, cf.c2, src.i, fabsf(src.amp));
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_scales_delta(g, pl.radius, st, cf.c2, src, stream);
   if (e != cudaSuccess) return e;
   return dispatch(storage, points, pl, a, maps, stream, nullptr);
+}
+
+cudaError_t launch_scales_delta(const Geom& g, int R, const Delta16Step& st, float c2, const Source& src,
+                                cudaStream_t stream) {
+  k_scales_delta<<<(g.xs + 255) / 256, 256, 0, stream>>>(g.xs, R, st.Mu, st.Md, st.Ms, st.Eu_out,
+                                                         st.Ed_out, st.Mu_out, st.Md_out, st.k4, c2,
+                                                         src.i, fabsf(src.amp));
+  return cudaGetLastError();
 }
 
 }  // namespace st3d

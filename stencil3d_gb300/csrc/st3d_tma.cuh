@@ -14,6 +14,8 @@ namespace st3d {
 constexpr int kTmaTK = 128;
 constexpr int kTmaKHalo = 4;                    // floats loaded either side along k (16 bytes)
 constexpr int kTmaUKW = kTmaTK + 2 * kTmaKHalo; // smem row width of a u tile
+// Columns per tile of the tensor-core 16-bit kernel (fifteen 8-column blocks).
+constexpr int kMmaTK = 120;
 
 struct TmaPlan {
   int tj = 16;      // rows per tile (consumer warps)
@@ -26,6 +28,18 @@ struct TmaPlan {
   uint64_t timeout_ns = 4000000000ull;
   CUtensorMap umap[5];  // halo box (kTmaUKW x (tj+2R) x 1) over each field buffer
   CUtensorMap vmap[5];  // interior box (kTmaTK x tj x 1) over each field buffer
+};
+
+// Per-plane record of the tensor-core 16-bit kernel (st3d_kernels_mma16.cu),
+// written before each step: the packed 16-bit weights (hi | hi << 16) of the
+// planes i-r (ihi/ilo[2r-2]) and i+r ([2r-1]), of d (wd) and s (wsh, wsl)
+// relative to 2^X, then 2^X, c1 * 2^(E_u - S), 2^E_u and the encode / decode
+// scales of the step's outputs.  128 bytes, one bulk copy.
+struct alignas(128) MmaRecord {
+  uint32_t ihi[8], ilo[8];
+  uint32_t wd, wsh, wsl;
+  float xs2, c1s, uc, inv_uo, inv_do, dq;
+  uint32_t pad[7];
 };
 
 // Plan of the 16-bit-storage kernels (st3d_kernels_tma16.cu for the
@@ -41,6 +55,10 @@ struct Tma16Plan {
   uint64_t timeout_ns = 4000000000ull;
   bool delta = false;     // FP16 / BF16 delta form (st3d_kernels_delta16.cu)
   bool pair = false;      // F16_HL: u as an FP16 hi/lo pair; lo[] are its lo words
+  bool mma = false;       // delta form on the tensor-core kernel (st3d_kernels_mma16.cu):
+                          // 16 x kMmaTK tiles, u box (kMmaTK+16) x 24, d/s/lo boxes kMmaTK x 16
+  int nb = 1;             // mma kernel: 8-column blocks per consumer warp
+  MmaRecord* mma_rec = nullptr;  // mma kernel: one record per i-plane (device)
   CUtensorMap uhi[2];
   CUtensorMap vhi[3];
   CUtensorMap lo[2];

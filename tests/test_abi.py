@@ -128,6 +128,21 @@ def test_plan_layout():
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", temporal_block=3), S.api.ERR_INVALID),
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", storage="f16", temporal_block=2),
      S.api.ERR_UNSUPPORTED),
+    # the tensor-core kernel: the 16-bit delta forms, 16-row tiles, 6/8/10 stages
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f16", kernel="mma"), S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", storage="bf16", kernel="mma"), S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", storage="f16_hl", kernel="mma", stages=8),
+     S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f32", kernel="mma"),
+     S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f16_hilo", kernel="mma"),
+     S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f16", kernel="mma", tile_j=20),
+     S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f16", kernel="mma", stages=4),
+     S.api.ERR_UNSUPPORTED),
+    ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f16_hl", kernel="mma", stages=6),
+     S.api.ERR_UNSUPPORTED),
 ])
 def test_plan_rejects_bad_requests(grid, opts, status):
     opts = dict(opts)
@@ -142,6 +157,14 @@ def test_plan_rejects_bad_requests(grid, opts, status):
     info = api.Info()
     rc = S.lib().st3d_plan(C.byref(S.Grid(*grid).desc()), C.byref(o), C.byref(info))
     assert rc == status, S.last_error()
+
+
+def test_plan_reports_the_tensor_core_kernel():
+    g = S.Grid(64, 64, 64, 4, 4, 4)
+    for storage in ("f16", "bf16", "f16_hl"):
+        info = S.plan(g, S.default_opts(25, "wave", storage, kernel="mma"))
+        assert info.kernel == S.KERNEL_MMA and info.tile_j == 16 and info.tile_k == 120
+    assert S.plan(g, S.default_opts(25, "wave", "f16", kernel="tma")).kernel == S.KERNEL_TMA
 
 
 def test_device_field_defaults_and_planning():
