@@ -66,6 +66,8 @@ TB_STEPS = {"wave13_1040": 2000}
 # host driver)
 CONFIG_RUNS = (("wave7_256", 20), ("wave25_528", 200))
 SEED = 20251203
+# st3d_kernel values by name
+KERNEL_NAMES = {1: "simple", 2: "tma", 3: "mma"}
 # CUDA device of this replica (LOCAL_RANK under torchrun)
 DEVICE = -1
 
@@ -468,6 +470,8 @@ def summary_of(result):
             continue
         out[form] = [_r(e["value"]), _r(e["speedup_vs_fp32"], 3), _r(e["roofline"]["frac"], 3),
                      _r(e.get("l2_err_vs_fp64"), 3)]
+        if e.get("kernel"):
+            out.setdefault("fp16_kernel", {})[form] = e["kernel"]
     b = result.get("batch")
     if b:
         out["batch"] = {"seq": _r(b["sequential"]["value"]), "persistent": _r(b["persistent"]["value"]),
@@ -644,8 +648,15 @@ def run_gb300(args, dist):
             result["fp16"][form] = {"value": gp, "unit": "Gpts/s", "ms_per_step": msf,
                                     "speedup_vs_fp32": gp / value,
                                     "bytes_per_point": finfo.bytes_per_point,
+                                    "kernel": KERNEL_NAMES.get(finfo.kernel, finfo.kernel),
                                     "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s",
                                                  "frac": ach / peak}}
+            if finfo.kernel == S.KERNEL_MMA:
+                # the scalar 16-bit kernel on the same workload, for comparison
+                gs, mss, _ = time_storage(S, args.workload, form, args.steps, args.warmup, "tma")
+                result["fp16"][form]["scalar_kernel"] = {
+                    "kernel": "tma", "value": dist.world * gs * (ms / ms_max), "ms_per_step": mss,
+                    "frac": finfo.bytes_per_point * pts / (mss * 1e-3) / 1e9 / peak}
     if args.fp64_steps > 0:
         # the reference's USE_DOUBLE build (config.h:96-97) on the device:
         # the plain kernel in FP64, 32 algorithmic bytes per point

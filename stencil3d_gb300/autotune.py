@@ -7,13 +7,16 @@ unit and the schedule (CUDA graph, plain persistent launches, or one
 pipelined launch per call).
 
 The knobs are the ``st3d_opts`` fields that change how the work is tiled,
-never what is computed: the kernel (TMA pipeline or plain), tile rows
-(``tile_j``), pipeline stages (``stages``), planes per work unit (``ichunk``)
-and, for the FP32 wave form of the 7- and 13-point stencils on a zero halo,
-steps fused per pass (``temporal_block``).  Every candidate produces the same
-bits as any other (the per-point operation sequence is fixed), so the tuner
-only ranks speed.  The reference has no counterpart (its tile sizes are
-command-line options, main.cpp:125-144).
+never what is computed: the kernel (TMA pipeline, plain, or for the 16-bit
+delta forms the tensor-core kernel), tile rows (``tile_j``), pipeline stages
+(``stages``), planes per work unit (``ichunk``) and, for the FP32 wave form
+of the 7- and 13-point stencils on a zero halo, steps fused per pass
+(``temporal_block``).  Every candidate produces the same bits as any other
+(the per-point operation sequence is fixed), except that the tensor-core
+kernel sums in the tensor cores' order (within one unit in the last place of
+the 16-bit words per step), so the tuner only ranks speed.  The reference
+has no counterpart (its tile sizes are command-line options,
+main.cpp:125-144).
 
     best = tune(Grid(1024, 1024, 1024, 4, 4, 4), 25, "wave", "f16")
     st = Stencil(grid, 25, "wave", "f16", **best["opts"])
@@ -45,12 +48,12 @@ def candidates(points, mode, storage, zero_halo=False):
         for tj, depths in ((16, (4, 6, 8)), (20, (6, 8)), (8, (4, 6, 8))):
             for nv in depths:
                 out.append({"kernel": "tma", "tile_j": tj, "stages": nv})
-        return out
+        return out + [{"kernel": "mma", "ichunk": ic} for ic in (0, 64, 256)]
     if storage in ("f16", "bf16"):
         for tj, depths in ((16, (4, 6, 8, 12)), (20, (6, 8, 10)), (8, (4, 6, 8, 12))):
             for nv in depths:
                 out.append({"kernel": "tma", "tile_j": tj, "stages": nv})
-        return out
+        return out + [{"kernel": "mma", "ichunk": ic} for ic in (0, 64, 256)]
     if storage == "f16_hilo":
         return [{"kernel": "tma", "tile_j": 16, "stages": nv} for nv in (4, 6, 8, 12)]
     if storage == "f64" or points == 2:

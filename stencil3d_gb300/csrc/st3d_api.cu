@@ -576,6 +576,20 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
   return ST3D_OK;
 }
 
+// The tensor-core kernel serves a delta-form request when asked for, or under
+// ST3D_KERNEL_AUTO where it is the faster kernel (measured at 1024^3 on a
+// GB300: 25 points FP16 423 against 317 Gpts/s, BF16 411 / 312, F16_HL 384 /
+// 283; 13 points FP16 473 / 408, BF16 454 / 399; the scalar TMA kernel stays
+// ahead for the 13-point pair form, 363 / 335, and at 7 points, 545 / 483)
+// and the request names no tile height or pipeline depth of the scalar one.
+bool mma_chosen(const st3d_opts& o) {
+  const bool delta = o.storage == ST3D_F16 || o.storage == ST3D_BF16 || o.storage == ST3D_F16_HL;
+  if (!delta || o.mode != ST3D_MODE_WAVE) return false;
+  if (o.kernel == ST3D_KERNEL_MMA) return true;
+  return o.kernel == ST3D_KERNEL_AUTO && o.tile_j == 0 && o.stages == 0 &&
+         (o.points == 25 || (o.points == 13 && o.storage != ST3D_F16_HL));
+}
+
 // Tensor-core delta-form plan (st3d_kernels_mma16.cu): 16-row x 120-column
 // tiles; tensor maps with a u box of 136 x 24 words (columns k0-8 .., rows
 // j0-R ..), d / s / lo boxes of 120 x 16 words, and interior boxes of 120 x
@@ -1211,7 +1225,7 @@ int st3d_plan(const st3d_grid_desc* grid, const st3d_opts* opts, st3d_info* info
   info->kernel = tma ? ST3D_KERNEL_TMA : ST3D_KERNEL_SIMPLE;
   info->tile_j = tma ? tj : 0;
   info->tile_k = tma ? kTmaTK : 0;
-  if (delta && opts->kernel == ST3D_KERNEL_MMA) {
+  if (delta && mma_chosen(*opts)) {
     info->kernel = ST3D_KERNEL_MMA;
     info->tile_j = 16;
     info->tile_k = kMmaTK;
@@ -1353,7 +1367,7 @@ int st3d::create_context(const st3d_grid_desc* grid, const st3d_opts* opts, cuda
     c->m2s = (float)(-2.0 * sw);
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-    const bool mma = c->delta && c->opts.kernel == ST3D_KERNEL_MMA;
+    const bool mma = c->delta && mma_chosen(c->opts);
     rc = mma ? plan_mma16(c, sm, max_smem) : plan_tma16(c, sm, max_smem);
     if (rc != ST3D_OK) return cleanup(rc);
     c->kernel = mma ? ST3D_KERNEL_MMA : ST3D_KERNEL_TMA;

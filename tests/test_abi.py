@@ -165,6 +165,14 @@ def test_plan_reports_the_tensor_core_kernel():
         info = S.plan(g, S.default_opts(25, "wave", storage, kernel="mma"))
         assert info.kernel == S.KERNEL_MMA and info.tile_j == 16 and info.tile_k == 120
     assert S.plan(g, S.default_opts(25, "wave", "f16", kernel="tma")).kernel == S.KERNEL_TMA
+    # AUTO: the tensor-core kernel where it is the faster one and no scalar
+    # tile or depth is named
+    auto = lambda p, st, **kw: S.plan(g, S.default_opts(p, "wave", st, **kw)).kernel
+    assert auto(25, "f16") == auto(25, "bf16") == auto(25, "f16_hl") == S.KERNEL_MMA
+    assert auto(13, "f16") == auto(13, "bf16") == S.KERNEL_MMA
+    assert auto(13, "f16_hl") == auto(7, "f16") == auto(7, "bf16") == S.KERNEL_TMA
+    assert auto(25, "f16", tile_j=20) == auto(25, "f16", stages=8) == S.KERNEL_TMA
+    assert auto(25, "f16_hilo") == auto(25, "f32") == S.KERNEL_TMA
 
 
 def test_device_field_defaults_and_planning():

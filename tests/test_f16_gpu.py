@@ -4,9 +4,11 @@
   - FP16 hi/lo pair: the delta form with u held as two FP16 words;
   - FP16 + a compensating byte: u and v in FP16 words plus a low byte.
 
-The library's 16-bit kernels and the oracle's restatement of the same
-encoding, scale rule and update must agree bit for bit (decoded u and v
-after several steps), for the 7-, 13- and 25-point stencils.  The 16-bit
+The library's scalar 16-bit kernels (kernel "tma") and the oracle's
+restatement of the same encoding, scale rule and update must agree bit for
+bit (decoded u and v after several steps), for the 7-, 13- and 25-point
+stencils; the tensor-core kernel of the delta forms is checked against the
+same restatement within rounding in tests/test_mma16_gpu.py.  The 16-bit
 forms keep a zero halo (a zero Dirichlet boundary); other halos are refused.
 """
 import numpy as np
@@ -41,7 +43,7 @@ def test_f16_forms_match_oracle(storage, points, grid, blobs):
     src = (grid[0] // 2, grid[1] // 2, grid[2] // 2)
     v, s, u = _inputs(grid, 3 + points, blobs)
     g = S.Grid(*grid)
-    with S.Stencil(g, points, "wave", storage, dt=dt, src=src) as st:
+    with S.Stencil(g, points, "wave", storage, dt=dt, src=src, kernel="tma") as st:
         assert st.info().kernel == S.KERNEL_TMA
         uu, vv = u.copy(), v.copy()
         st.iterate_host(vv, s, uu, steps)
@@ -63,7 +65,7 @@ def test_delta_form_tiles_match_oracle(points, storage, tile_j, stages):
     src = (15, 21, 70)
     v, s, u = _inputs(grid, 40 + points, True)
     with S.Stencil(S.Grid(*grid), points, "wave", storage, dt=dt, src=src, tile_j=tile_j,
-                   stages=stages) as st:
+                   stages=stages, kernel="tma") as st:
         assert st.info().tile_j == tile_j
         uu, vv = u.copy(), v.copy()
         st.iterate_host(vv, s, uu, steps)
