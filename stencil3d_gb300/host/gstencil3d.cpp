@@ -10,7 +10,7 @@
 //
 // Added flags: --stencil N (2, 7, 13, 25; default 7 as config.h:38),
 // --wave (the leapfrog form, README.md:11-20, with --vel/--dt/--dx),
-// --kernel simple|tma|auto, --variant ref|vec8|vec16 (the reference's
+// --kernel simple|tma|mma|auto, --variant ref|vec8|vec16 (the reference's
 // compile-time kernel variant whose results to reproduce), --storage
 // f32|f16|bf16|f16_hilo|f16_hl (device storage of the wave form) and
 // --temporal-block 1|2|4 (FP32 wave steps fused per pass).
@@ -150,6 +150,7 @@ int main(int argc, char** argv) {
   gopt.mode = wave ? ST3D_MODE_WAVE : ST3D_MODE_REF;
   gopt.kernel = strcmp(kernel, "simple") == 0 ? ST3D_KERNEL_SIMPLE
               : strcmp(kernel, "tma") == 0    ? ST3D_KERNEL_TMA
+              : strcmp(kernel, "mma") == 0    ? ST3D_KERNEL_MMA
                                               : ST3D_KERNEL_AUTO;
   gb300_configure(gopt);
 
