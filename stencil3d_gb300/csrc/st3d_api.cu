@@ -169,8 +169,9 @@ int validate(const st3d_grid_desc* g, const st3d_opts* o) {
     return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel serves the 16-bit delta forms (F16, BF16, F16_HL)");
   if (o->kernel == ST3D_KERNEL_MMA && o->tile_j != 0 && o->tile_j != 16)
     return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel runs 16-row tiles, not %d", o->tile_j);
-  if (o->kernel == ST3D_KERNEL_MMA && o->stages != 0 && o->stages != 8)
-    return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel runs 8 stages, not %d", o->stages);
+  if (o->kernel == ST3D_KERNEL_MMA && o->stages != 0 && o->stages != (o->storage == ST3D_F16_HL ? 4 : 8))
+    return fail(ST3D_ERR_UNSUPPORTED, "the tensor-core kernel runs %d stages, not %d",
+                o->storage == ST3D_F16_HL ? 4 : 8, o->stages);
   if (o->kernel == ST3D_KERNEL_TMA && o->storage == ST3D_F64)
     return fail(ST3D_ERR_UNSUPPORTED, "the TMA kernel serves FP32 and 16-bit storage");
   if (o->kernel == ST3D_KERNEL_TMA && o->points == 2)
@@ -577,23 +578,24 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
 }
 
 // The tensor-core kernel serves a delta-form request when asked for, or under
-// ST3D_KERNEL_AUTO where it is the faster kernel (measured at 1024^3 on a
-// GB300: 25 points FP16 423 against 317 Gpts/s, BF16 411 / 312, F16_HL 384 /
-// 283; 13 points FP16 473 / 408, BF16 454 / 399; the scalar TMA kernel stays
-// ahead for the 13-point pair form, 363 / 335, and at 7 points, 545 / 483)
-// and the request names no tile height or pipeline depth of the scalar one.
+// ST3D_KERNEL_AUTO when the request names no tile height or pipeline depth of
+// the scalar kernel: measured at 1024^3 on a GB300 it is the faster kernel
+// of the delta forms (25 points FP16 458 against 317 Gpts/s, BF16 447 / 312,
+// F16_HL 394 / 283; 13 points (1040^3) FP16 523 / 408, F16_HL 404 / 363;
+// 7 points FP16 549 / 545, F16_HL 416 / 357) but for 7-point BF16, 523 /
+// 531.
 bool mma_chosen(const st3d_opts& o) {
   const bool delta = o.storage == ST3D_F16 || o.storage == ST3D_BF16 || o.storage == ST3D_F16_HL;
   if (!delta || o.mode != ST3D_MODE_WAVE) return false;
   if (o.kernel == ST3D_KERNEL_MMA) return true;
-  return o.kernel == ST3D_KERNEL_AUTO && o.tile_j == 0 && o.stages == 0 &&
-         (o.points == 25 || (o.points == 13 && o.storage != ST3D_F16_HL));
+  return o.kernel == ST3D_KERNEL_AUTO && o.tile_j == 0 && o.stages == 0;
 }
 
-// Tensor-core delta-form plan (st3d_kernels_mma16.cu): 16-row x 120-column
-// tiles; tensor maps with a u box of 136 x 24 words (columns k0-8 .., rows
-// j0-R ..), d / s / lo boxes of 120 x 16 words, and interior boxes of 120 x
-// 16 over the u buffers for the stores of u^{n+1}.
+// Tensor-core delta-form plan (st3d_kernels_mma16.cu): 16-row x 152-column
+// tiles; tensor maps with a u box of 168 x 24 words (columns k0-8 .., rows
+// j0-R ..), d / s / lo boxes of 152 x 16 words, and interior boxes of 152 x
+// 16 over the u buffers for the stores of u^{n+1}; 8 pipeline stages (4 for
+// the pair form).
 int plan_mma16(st3d_ctx* c, int sm_count, int max_smem) {
   Tma16Plan* p = new (std::nothrow) Tma16Plan();
   if (!p) return fail(ST3D_ERR_NOMEM, "host allocation failed");
@@ -604,7 +606,7 @@ int plan_mma16(st3d_ctx* c, int sm_count, int max_smem) {
   p->pair = c->pair;
   p->mma = true;
   p->nb = 1;
-  p->nv = 8;
+  p->nv = c->pair ? 4 : 8;
   p->smem = mma16_smem_bytes(p->nv, R, c->pair);
   const int per_sm =
       (int)p->smem <= max_smem ? mma16_blocks_per_sm(c->opts.storage, c->opts.points, *p) : 0;
@@ -625,7 +627,7 @@ int plan_mma16(st3d_ctx* c, int sm_count, int max_smem) {
   p->nti = (int)((c->L.xs + p->ichunk - 1) / p->ichunk);
   p->units = p->ntj * p->ntk * p->nti;
   p->grid = ctas < p->units ? ctas : p->units;
-  p->threads = 16 * 32;
+  p->threads = (kMmaTK / 8 + 1) * 32;
   const CUtensorMapDataType w16 =
       c->opts.storage == ST3D_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
   int ok = ST3D_OK;

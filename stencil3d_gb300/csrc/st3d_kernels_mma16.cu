@@ -36,13 +36,15 @@
 // near a rounding boundary.  Weights below the FP16 range relative to the
 // plane's largest (2^-38 of it) drop out, far below FP32 rounding of the sum.
 //
-// Structure (one CTA per SM, persistent over 16-row x 120-column x
+// Structure (one CTA per SM, persistent over 16-row x 152-column x
 // ichunk-plane units): a producer thread streams, per step, the u plane i+R
-// (rows j0-R .. j0-R+23, columns k0-8 .. k0+127) and, for the centre plane
-// i, d, s (the lo words of u) over columns k0 .. k0+119 and the plane's
-// record, through an mbarrier ring of 8 stages; 15 consumer warps each own
-// one 16x8 block.  The row pitches (272 and 240 bytes) put the eight rows of
-// every ldmatrix in distinct banks.  Each warp writes its block of u^{n+1},
+// (rows j0-R .. j0-R+23, columns k0-8 .. k0+159) and, for the centre plane
+// i, d, s (the lo words of u) over columns k0 .. k0+151 and the plane's
+// record, through an mbarrier ring of 8 stages (4 for the pair form); 19
+// consumer warps each own one 16x8 block (20 warps with the producer: five
+// on some schedulers, within the 96 registers a thread that leaves; the
+// kernel takes 81-87).  The row pitches (336 and 304 bytes) put the eight
+// rows of every ldmatrix in distinct banks.  Each warp writes its block of u^{n+1},
 // d^{n+1} (and the lo words) into the stage's s, d (and lo) slots, whose
 // inputs it has read, with zero words at the points outside the grid; once
 // every warp has released the stage the producer stores the three tiles with
@@ -67,12 +69,13 @@ namespace st3d {
 namespace {
 
 constexpr int kMTJ = 16;         // rows per tile (one 16-row mma block)
-constexpr int kMTK = kMmaTK;     // columns per tile (fifteen 8-column blocks)
+constexpr int kMTK = kMmaTK;     // columns per tile (nineteen 8-column blocks)
 constexpr int kMCW = kMmaTK / 8; // consumer warps, one 8-column block each
-constexpr int kMUW = kMTK + 16;  // u tile row: k0-8 .. k0+127, 272 bytes
-constexpr int kMVW = kMTK;       // d / s / lo tile row: k0 .. k0+119, 240 bytes
+constexpr int kMUW = kMTK + 16;  // u tile row: k0-8 .. k0+159, 336 bytes
+constexpr int kMVW = kMTK;       // d / s / lo tile row: k0 .. k0+151, 304 bytes
 constexpr int kMUH = kMTJ + 8;   // u tile rows: j0-R .. j0-R+23
-constexpr int kMNV = 8;          // pipeline stages
+constexpr int kMNV = 8;          // pipeline stages (4 for the pair form, whose third tile per stage
+                                 // would not fit 8)
 constexpr int kMNU = 16;         // u ring slots (>= NV + 2R; a power of two)
 
 template <int P>
@@ -244,7 +247,7 @@ __global__ void __launch_bounds__((kMCW + 1) * 32, 1)
             const __grid_constant__ CUtensorMap uomap, const __grid_constant__ CUtensorMap lomap,
             const Mma16Args a) {
   constexpr int R = RadM<P>::value;
-  constexpr int NV = kMNV;
+  constexpr int NV = PAIR ? kMNV / 2 : kMNV;
   constexpr int NU = kMNU;
   constexpr int CW = kMCW;
   constexpr uint32_t UBYTES = kMUW * kMUH * 2;
@@ -609,7 +612,7 @@ __global__ void k_mma_records(int xs, int R, const int* __restrict__ Eu, const i
 template <int KIND, int P, bool PAIR>
 cudaError_t launch_p(const Tma16Plan& pl, const Mma16Args& args, const CUtensorMap* maps,
                      cudaStream_t stream, int* occupancy_out) {
-  if (pl.nv != kMNV || pl.nb != 1) return cudaErrorInvalidConfiguration;
+  if (pl.nv != (PAIR ? kMNV / 2 : kMNV) || pl.nb != 1) return cudaErrorInvalidConfiguration;
   auto kern = k_mma16<KIND, P, PAIR>;
   const int threads = (kMCW + 1) * 32;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);

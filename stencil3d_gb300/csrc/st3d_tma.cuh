@@ -14,8 +14,9 @@ namespace st3d {
 constexpr int kTmaTK = 128;
 constexpr int kTmaKHalo = 4;                    // floats loaded either side along k (16 bytes)
 constexpr int kTmaUKW = kTmaTK + 2 * kTmaKHalo; // smem row width of a u tile
-// Columns per tile of the tensor-core 16-bit kernel (fifteen 8-column blocks).
-constexpr int kMmaTK = 120;
+// Columns per tile of the tensor-core 16-bit kernel (nineteen 8-column
+// blocks, one consumer warp each).
+constexpr int kMmaTK = 152;
 
 struct TmaPlan {
   int tj = 16;      // rows per tile (consumer warps)

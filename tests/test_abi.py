@@ -131,8 +131,12 @@ def test_plan_layout():
     # the tensor-core kernel: the 16-bit delta forms, 16-row tiles, 6/8/10 stages
     ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f16", kernel="mma"), S.api.OK),
     ((8, 8, 8, 4, 4, 4), dict(points=7, mode="wave", storage="bf16", kernel="mma"), S.api.OK),
-    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", storage="f16_hl", kernel="mma", stages=8),
+    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", storage="f16_hl", kernel="mma", stages=4),
      S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", storage="f16", kernel="mma", stages=8),
+     S.api.OK),
+    ((8, 8, 8, 4, 4, 4), dict(points=13, mode="wave", storage="f16_hl", kernel="mma", stages=8),
+     S.api.ERR_UNSUPPORTED),
     ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f32", kernel="mma"),
      S.api.ERR_UNSUPPORTED),
     ((8, 8, 8, 4, 4, 4), dict(points=25, mode="wave", storage="f16_hilo", kernel="mma"),
@@ -163,14 +167,13 @@ def test_plan_reports_the_tensor_core_kernel():
     g = S.Grid(64, 64, 64, 4, 4, 4)
     for storage in ("f16", "bf16", "f16_hl"):
         info = S.plan(g, S.default_opts(25, "wave", storage, kernel="mma"))
-        assert info.kernel == S.KERNEL_MMA and info.tile_j == 16 and info.tile_k == 120
+        assert info.kernel == S.KERNEL_MMA and info.tile_j == 16 and info.tile_k == 152
     assert S.plan(g, S.default_opts(25, "wave", "f16", kernel="tma")).kernel == S.KERNEL_TMA
-    # AUTO: the tensor-core kernel where it is the faster one and no scalar
-    # tile or depth is named
+    # AUTO: the tensor-core kernel for the delta forms when no scalar tile or
+    # depth is named
     auto = lambda p, st, **kw: S.plan(g, S.default_opts(p, "wave", st, **kw)).kernel
-    assert auto(25, "f16") == auto(25, "bf16") == auto(25, "f16_hl") == S.KERNEL_MMA
-    assert auto(13, "f16") == auto(13, "bf16") == S.KERNEL_MMA
-    assert auto(13, "f16_hl") == auto(7, "f16") == auto(7, "bf16") == S.KERNEL_TMA
+    for p in (7, 13, 25):
+        assert auto(p, "f16") == auto(p, "bf16") == auto(p, "f16_hl") == S.KERNEL_MMA
     assert auto(25, "f16", tile_j=20) == auto(25, "f16", stages=8) == S.KERNEL_TMA
     assert auto(25, "f16_hilo") == auto(25, "f32") == S.KERNEL_TMA
 
