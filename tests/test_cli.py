@@ -104,7 +104,8 @@ def test_storage_needs_the_wave_form():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("extra", [["--storage", "f16"], ["--storage", "f16_hilo"],
-                                   ["--storage", "f16_hl"],
+                                   ["--storage", "f16_hl"], ["--storage", "bf16", "--kernel", "mma"],
+                                   ["--storage", "f16", "--kernel", "tma"],
                                    ["--stencil", "7", "--temporal-block", "4"]])
 def test_wave_forms_through_the_driver(extra):
     args = ["--xs", "40", "--ys", "40", "--zs", "128", "--iter", "8", "--wave", "--dt", "0.0005"]
