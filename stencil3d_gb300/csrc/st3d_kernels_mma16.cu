@@ -175,6 +175,9 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 __device__ __forceinline__ void bulk_wait_read0() {
   asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
+__device__ __forceinline__ void bulk_wait_read1() {
+  asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // w -> (hi, lo) 16-bit words with hi = rn16(w), lo = rn16(w - hi)
@@ -295,15 +298,37 @@ __global__ void __launch_bounds__((kMCW + 1) * 32, 1)
     if (lane != 0) return;
     // The outputs of a finished step sit in its stage's d (d^{n+1}), s
     // (u^{n+1}) and lo slots; they go out as tile stores, clipped to the
-    // interior by the tensor maps, and have been read out of shared memory
-    // before the slots are loaded again.
-    auto store_outputs = [&](int stage, int i) {
-      const int x = g.pk + sk0[stage], y = g.pj + sj0[stage], z = g.pi + i;
-      tma_store_3d(&uomap, sr + stage * VSLOT, x, y, z);
-      tma_store_3d(&dmap, dr + stage * VSLOT, x, y, z);
-      if (PAIR) tma_store_3d(&lomap, lr + stage * VSLOT, x, y, z);
-      bulk_commit();
-      bulk_wait_read0();
+    // interior by the tensor maps.  A step is retired (its consumers done,
+    // its stores issued, its maxima flushed) one step before its stage is
+    // loaded again, so that by then the stores have read the slots and the
+    // wait for that is short (7-point FP16 549 -> 613 Gpts/s at 1024^3); the
+    // pair form's 4-stage ring retires a step just before the reload
+    // instead (one step early it loses a quarter of its depth: 394 -> 351
+    // at 25 points).
+    uint32_t hr = 0;           // next step to retire
+    bool stored = false;       // the last retired step issued stores
+    auto retire = [&]() -> bool {
+      const uint32_t m = hr++;
+      const int stage = (int)(m & (NV - 1));
+      if (!mbar_wait_bounded(&empty[stage], (m / NV) & 1u, a.timeout_ns)) {
+        atomicExch(a.status, (uint32_t)kDevTimeoutEmpty);
+        stored = false;
+        return false;
+      }
+      stored = splane[stage] >= 0;
+      if (stored) {
+        const int i = splane[stage];
+        const int x = g.pk + sk0[stage], y = g.pj + sj0[stage], z = g.pi + i;
+        tma_store_3d(&uomap, sr + stage * VSLOT, x, y, z);
+        tma_store_3d(&dmap, dr + stage * VSLOT, x, y, z);
+        if (PAIR) tma_store_3d(&lomap, lr + stage * VSLOT, x, y, z);
+        bulk_commit();
+        if (smax_u[stage]) atomicMax(&a.Mu_out[i], smax_u[stage]);
+        if (smax_d[stage]) atomicMax(&a.Md_out[i], smax_d[stage]);
+        smax_u[stage] = 0u;
+        smax_d[stage] = 0u;
+      }
+      return true;
     };
     tma_prefetch_desc(&umap);
     tma_prefetch_desc(&dmap);
@@ -322,18 +347,28 @@ __global__ void __launch_bounds__((kMCW + 1) * 32, 1)
       const int nsteps = (ib - ia) + 2 * R;
       for (int n = 0; n < nsteps; ++n, ++h) {
         const int stage = (int)(h & (NV - 1));
-        if (h >= (uint32_t)NV) {
-          if (!mbar_wait_bounded(&empty[stage], ((h / NV) - 1) & 1u, a.timeout_ns)) {
-            atomicExch(a.status, (uint32_t)kDevTimeoutEmpty);
-            ok = false;
-            break;
+        if constexpr (NV >= 8) {
+          // retire the step whose stage is loaded next (h + 1 - NV); the
+          // stores of this stage's last step (h - NV) were issued one step
+          // ago: wait until at most the group just issued still reads
+          if (h + 1 >= (uint32_t)NV) {
+            if (!retire()) {
+              ok = false;
+              break;
+            }
+            if (stored) bulk_wait_read1();
+            else bulk_wait_read0();
           }
-          if (splane[stage] >= 0) {
-            store_outputs(stage, splane[stage]);
-            if (smax_u[stage]) atomicMax(&a.Mu_out[splane[stage]], smax_u[stage]);
-            if (smax_d[stage]) atomicMax(&a.Md_out[splane[stage]], smax_d[stage]);
-            smax_u[stage] = 0u;
-            smax_d[stage] = 0u;
+        } else {
+          // a shallow ring (the pair form's 4 stages) keeps every stage in
+          // flight: retire this stage's last step (h - NV) and wait for its
+          // stores' reads
+          if (h >= (uint32_t)NV) {
+            if (!retire()) {
+              ok = false;
+              break;
+            }
+            bulk_wait_read0();
           }
         }
         const int p = ia - R + n;
@@ -353,19 +388,16 @@ __global__ void __launch_bounds__((kMCW + 1) * 32, 1)
         }
       }
     }
-    // Drain: no copy in flight, every stage consumed, maxima flushed.
-    for (uint32_t m = (h > (uint32_t)NV ? h - NV : 0u); m < h; ++m) {
-      const int stage = (int)(m & (NV - 1));
-      const bool landed = mbar_wait_bounded(&full[stage], (m / NV) & 1u, a.timeout_ns);
-      if (!landed || !mbar_wait_bounded(&empty[stage], (m / NV) & 1u, a.timeout_ns)) {
+    // Drain: no copy in flight, every step retired (stores issued, maxima
+    // flushed), then every store complete.
+    while (hr < h) {
+      const uint32_t m = hr;
+      if (!mbar_wait_bounded(&full[m & (NV - 1)], (m / NV) & 1u, a.timeout_ns)) {
         atomicExch(a.status, (uint32_t)kDevTimeoutEmpty);
+        ++hr;
         continue;
       }
-      if (splane[stage] >= 0) {
-        store_outputs(stage, splane[stage]);
-        if (smax_u[stage]) atomicMax(&a.Mu_out[splane[stage]], smax_u[stage]);
-        if (smax_d[stage]) atomicMax(&a.Md_out[splane[stage]], smax_d[stage]);
-      }
+      retire();
     }
     bulk_wait_all();
     return;
