@@ -490,24 +490,25 @@ __global__ void __launch_bounds__((kMCW + 1) * 32, 1)
           mma_k8<KIND>(Dk, Y0, Y1, wkh[2]);
           mma_k8<KIND>(Dj, wjh[4], wjh[5], B[2]);
         }
-        // Dr: the i pairs, d and s with the plane's weights
-        float Dr[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        // d and s with the plane's weights, then the i pairs: per radius
+        // [U_{i-r} | U_{i+r}] x [diag(2^(E_{i-r}-X)) ; diag(2^(E_{i+r}-X))]
+        // (exact products) times c1 w_r 2^X in FP32
         float Ds[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         mma_k16<KIND>(Ds, DS[0], DS[1], DS[2], DS[3], W.wd & dmask, W.wsh & dmask);
         mma_k8<KIND>(Ds, DS[2], DS[3], W.wsl & dmask);
+        const float2 ys2 = splat(W.ys2), c1s = splat(W.c1s);
+        const float2 jk01 = __fadd2_rn(make_float2(Dk[0], Dk[1]), make_float2(Dj[0], Dj[1]));
+        const float2 jk23 = __fadd2_rn(make_float2(Dk[2], Dk[3]), make_float2(Dj[2], Dj[3]));
+        P4 dn = {__ffma2_rn(jk01, c1s, __fmul2_rn(make_float2(Ds[0], Ds[1]), ys2)),
+                 __ffma2_rn(jk23, c1s, __fmul2_rn(make_float2(Ds[2], Ds[3]), ys2))};
 #pragma unroll
         for (int r = 1; r <= R; ++r) {
           uint32_t Q[4];
           ldsm_x4(Q, pbase + ((hh - R + rsign * r) & (NU - 1)) * USLOT);
-          mma_k16<KIND>(Dr, Q[0], Q[1], Q[2], Q[3], W.ihi[2 * r - 2] & dmask, W.ihi[2 * r - 1] & dmask);
-          mma_k16<KIND>(Dr, Q[0], Q[1], Q[2], Q[3], W.ilo[2 * r - 2] & dmask, W.ilo[2 * r - 1] & dmask);
+          float Pr[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+          mma_k16<KIND>(Pr, Q[0], Q[1], Q[2], Q[3], W.ipw[2 * r - 2] & dmask, W.ipw[2 * r - 1] & dmask);
+          dn = fma4(splat(W.ci[r - 1]), P4{make_float2(Pr[0], Pr[1]), make_float2(Pr[2], Pr[3])}, dn);
         }
-        const float2 xs2 = splat(W.xs2), c1s = splat(W.c1s);
-        const float2 rr01 = __fadd2_rn(make_float2(Dr[0], Dr[1]), make_float2(Ds[0], Ds[1]));
-        const float2 rr23 = __fadd2_rn(make_float2(Dr[2], Dr[3]), make_float2(Ds[2], Ds[3]));
-        const float2 jk01 = __fadd2_rn(make_float2(Dk[0], Dk[1]), make_float2(Dj[0], Dj[1]));
-        const float2 jk23 = __fadd2_rn(make_float2(Dk[2], Dk[3]), make_float2(Dj[2], Dj[3]));
-        P4 dn = {__ffma2_rn(jk01, c1s, __fmul2_rn(rr01, xs2)), __ffma2_rn(jk23, c1s, __fmul2_rn(rr23, xs2))};
         // the centre u: the hi words (X[2], X[3]) and, for the pair form, the lo words
         P4 u0 = decode4<KIND>(make_uint2(X[2], X[3]), W.uc);
         if (PAIR) {
@@ -600,44 +601,46 @@ __global__ void k_mma_records(int xs, int R, const int* __restrict__ Eu, const i
   Eu_out[i] = euo;
   Mu_out[i] = 0u;
   Md_out[i] = 0u;
-  // the weights of the i planes, d and s, before the common factor 2^-X
+  // the i planes: their scales relative to 2^X, X = the largest of them
+  // less 15, as exact 16-bit powers of two (a plane 2^-24 or more below the
+  // largest one takes 0: its contribution is below FP32 rounding of the sum)
   const float w[5] = {0.0f, wi.x, wi.y, wi.z, wi.w};
-  float mag[10];
+  int ep[8];
+  int emax = -100000;
   for (int r = 1; r <= 4; ++r)
     for (int side = 0; side < 2; ++side) {
       const int p = side ? i + r : i - r;
-      mag[2 * r - 2 + side] = (r <= R && p >= 0 && p < xs) ? ldexpf(c1 * w[r], Eu[p]) : 0.0f;
+      const bool in = r <= R && p >= 0 && p < xs;
+      ep[2 * r - 2 + side] = in ? Eu[p] : -100000;
+      if (in) emax = max(emax, Eu[p]);
     }
-  mag[8] = ldexpf(1.0f, Ed[i]);
-  mag[9] = ldexpf(c2, Es[i]);
-  int emax = -100000;
-  for (int m = 0; m < 10; ++m)
-    if (mag[m] != 0.0f) {
-      int e;
-      frexpf(mag[m], &e);
-      emax = max(emax, e);
-    }
-  const int X = emax == -100000 ? 0 : emax - 14;  // the largest |v| in [2^13, 2^14)
+  const int X = emax == -100000 ? 0 : emax - 15;
   MmaRecord o;
   for (int m = 0; m < 8; ++m) {
-    uint32_t hi, lo;
-    split16<KIND>(ldexpf(mag[m], -X), hi, lo);
-    o.ihi[m] = hi | (hi << 16);
-    o.ilo[m] = lo | (lo << 16);
+    uint32_t p2 = 0u, unused;
+    if (ep[m] != -100000 && ep[m] - X >= -40) split16<KIND>(ldexpf(1.0f, ep[m] - X), p2, unused);
+    o.ipw[m] = p2 | (p2 << 16);
   }
+  for (int r = 1; r <= 4; ++r) o.ci[r - 1] = ldexpf(c1 * w[r], X);
+  // d and s relative to 2^Y, the larger of them in [2^13, 2^14)
+  const float md = ldexpf(1.0f, Ed[i]), ms = ldexpf(c2, Es[i]);
+  int e1 = 0, e2 = 0;
+  frexpf(md, &e1);
+  if (ms != 0.0f) frexpf(ms, &e2);
+  const int Y = (ms != 0.0f ? max(e1, e2) : e1) - 14;
   uint32_t hi, lo;
-  split16<KIND>(ldexpf(mag[8], -X), hi, lo);
+  split16<KIND>(ldexpf(md, -Y), hi, lo);
   o.wd = hi | (hi << 16);
-  split16<KIND>(ldexpf(mag[9], -X), hi, lo);
+  split16<KIND>(ldexpf(ms, -Y), hi, lo);
   o.wsh = hi | (hi << 16);
   o.wsl = lo | (lo << 16);
-  o.xs2 = ldexpf(1.0f, X);
+  o.ys2 = ldexpf(1.0f, Y);
   o.c1s = ldexpf(c1, Eu[i] - S);
   o.uc = exp2i(Eu[i]);
   o.inv_uo = exp2i(-euo);
   o.inv_do = exp2i(-edo);
   o.dq = exp2i(edo);
-  for (int m = 0; m < 7; ++m) o.pad[m] = 0u;
+  for (int m = 0; m < 11; ++m) o.pad[m] = 0u;
   rec[i] = o;
 }
 

@@ -32,15 +32,17 @@ struct TmaPlan {
 };
 
 // Per-plane record of the tensor-core 16-bit kernel (st3d_kernels_mma16.cu),
-// written before each step: the packed 16-bit weights (hi | hi << 16) of the
-// planes i-r (ihi/ilo[2r-2]) and i+r ([2r-1]), of d (wd) and s (wsh, wsl)
-// relative to 2^X, then 2^X, c1 * 2^(E_u - S), 2^E_u and the encode / decode
-// scales of the step's outputs.  128 bytes, one bulk copy.
+// written before each step: ipw, the scales of the planes i-r (ipw[2r-2])
+// and i+r (ipw[2r-1]) relative to 2^X as exact 16-bit powers of two
+// (packed p | p << 16); ci[r-1] = c1 * w_r * 2^X; the weights of d (wd) and
+// s (wsh, wsl) relative to 2^Y; then 2^Y, c1 * 2^(E_u - S), 2^E_u and the
+// encode / decode scales of the step's outputs.  128 bytes, one bulk copy.
 struct alignas(128) MmaRecord {
-  uint32_t ihi[8], ilo[8];
+  uint32_t ipw[8];
+  float ci[4];
   uint32_t wd, wsh, wsl;
-  float xs2, c1s, uc, inv_uo, inv_do, dq;
-  uint32_t pad[7];
+  float ys2, c1s, uc, inv_uo, inv_do, dq;
+  uint32_t pad[11];
 };
 
 // Plan of the 16-bit-storage kernels (st3d_kernels_tma16.cu for the
