@@ -16,15 +16,19 @@
 //     columns; Wj[m][c] = w_j(c - R - m), w_j(0) = 0), constant band
 //     matrices of w * 2^S held as 16-bit hi/lo pairs (S puts the largest
 //     weight near 2^14; hi + lo carries a weight to ~22 bits, ~16 for BF16);
-//   - Dr, the i pairs, d and s: [U_{i-r} | U_{i+r}] * [diag(v_-); diag(v_+)]
-//     for r = 1..R and [D | S] * [diag(v_d); diag(v_s)], where each v is the
-//     plane's weight times its scale relative to 2^X (v_{i+e} =
-//     c1 w_e 2^(E_{i+e} - X), v_d = 2^(E_d - X), v_s = c2 2^(E_s - X)), X
-//     chosen per plane so that the largest v lies in [2^13, 2^14);
-//   - d^{n+1} = Djk * c1 2^(E_i - S) + Dr * 2^X.
-// The per-plane weights (hi/lo words), 2^X and the step's other scales form
-// one 128-byte record per plane, written before each step by k_mma_records
-// and brought into the stage by the producer with one bulk copy.  The u
+//   - Ds, d and s: [D | S] * [diag(v_d); diag(v_s)] with v_d = 2^(E_d - Y)
+//     and v_s = c2 2^(E_s - Y) (hi/lo words; Y puts the larger in
+//     [2^13, 2^14));
+//   - Pr, the i pair at radius r: [U_{i-r} | U_{i+r}] * [diag(2^(E_{i-r}-X));
+//     diag(2^(E_{i+r}-X))], the planes' scales relative to 2^X (X = the
+//     largest of them less 15) as exact 16-bit powers of two, so the
+//     products are exact and one mma per radius carries the pair;
+//   - d^{n+1} = Djk * c1 2^(E_i - S) + Ds * 2^Y + sum_r (c1 w_r 2^X) * Pr in
+//     FP32.
+// The per-plane weights, 2^X-scaled factors c1 w_r 2^X, 2^Y and the step's
+// other scales form one 128-byte record per plane, written before each step
+// by k_mma_records and brought into the stage by the producer with one bulk
+// copy.  The u
 // planes i-R .. i+R all stay in the shared-memory ring (16 slots >= 8 stages
 // + 2R), so no register queue along i is needed.  The centre u (and, for the
 // pair form, its lo words) is decoded in FP32 for u^{n+1} = u + dec(enc(d)).
@@ -33,8 +37,9 @@
 // kernel is not bit-identical to the scalar one or to the oracle's
 // restatement: a step agrees with them to FP32 rounding of the sum, and the
 // 16-bit words of u and d to one unit in the last place where the sum falls
-// near a rounding boundary.  Weights below the FP16 range relative to the
-// plane's largest (2^-38 of it) drop out, far below FP32 rounding of the sum.
+// near a rounding boundary.  A neighbour plane whose scale lies 2^-24 or
+// more below the largest of them (2^-40 for BF16) takes a zero weight: its
+// contribution is far below FP32 rounding of the sum.
 //
 // Structure (one CTA per SM, persistent over 16-row x 152-column x
 // ichunk-plane units): a producer thread streams, per step, the u plane i+R
