@@ -38,9 +38,9 @@
 // restatement: a step agrees with them to FP32 rounding of the sum, and the
 // 16-bit words of u and d to one unit in the last place where the sum falls
 // near a rounding boundary.  A neighbour plane whose scale lies more than
-// 2^39 below the largest of them (2^24 for FP16 weights, whose powers of two
-// end there) takes a zero weight: its contribution is far below FP32
-// rounding of the sum.
+// 2^39 below the largest of them (2^55 for BF16) takes a zero weight (the
+// FP16 powers of two end at 2^-24 = 2^(39-15) below 2^X): its contribution
+// is far below FP32 rounding of the sum.
 //
 // Structure (one CTA per SM, persistent over 16-row x 152-column x
 // ichunk-plane units): a producer thread streams, per step, the u plane i+R
@@ -608,8 +608,8 @@ __global__ void k_mma_records(int xs, int R, const int* __restrict__ Eu, const i
   Mu_out[i] = 0u;
   Md_out[i] = 0u;
   // the i planes: their scales relative to 2^X, X = the largest of them
-  // less 15, as exact 16-bit powers of two (a plane more than 2^24 below the
-  // largest, 2^39 for BF16, takes 0: its contribution is below FP32 rounding
+  // less 15, as exact 16-bit powers of two (a plane more than 2^39 below the
+  // largest, 2^55 for BF16, takes 0: its contribution is below FP32 rounding
   // of the sum)
   const float w[5] = {0.0f, wi.x, wi.y, wi.z, wi.w};
   int ep[8];
