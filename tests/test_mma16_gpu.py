@@ -129,3 +129,31 @@ def test_mma_tracks_tma_kernel_on_ragged_rows(storage, zs):
         b.download(u=ub)
     assert rel_l2(O.interior(ua, grid), O.interior(ub, grid)) < 2e-4
     assert np.all(ua[:, :, :4] == 0.0) and np.all(ua[:, :, 4 + zs:] == 0.0)
+
+
+@pytest.mark.parametrize("storage", ["f16", "f16_hl", "bf16"])
+def test_mma_plane_scales_far_apart(storage):
+    """Planes whose scales differ by about 2^40 along i (a blob field and the
+    same field times 1e-12): the i-pair weights are the planes' scales as
+    exact 16-bit powers of two relative to the largest neighbour, and a plane
+    too far below it takes a zero weight.  One step stays within one unit in
+    the last place of the oracle's restatement at every point, on both
+    sides of the jump."""
+    grid = (24, 30, 70, 4, 4, 4)
+    v, s, u = _inputs(grid, 9, True)
+    scale = np.ones(u.shape, np.float32)
+    scale[4 + 12:] = np.float32(1e-12)
+    u = (u * scale).astype(np.float32)
+    v = (v * scale).astype(np.float32)
+    dt, src = 5e-4, None
+    with S.Stencil(S.Grid(*grid), 25, "wave", storage, dt=dt, src=src, kernel="mma") as st:
+        uu, vv = u.copy(), v.copy()
+        st.iterate_host(vv, s, uu, 1)
+    ou, ov = _oracle_run(storage, u, v, s, grid, 25, 1, dt, src)
+    ui, oui, ovi = O.interior(uu, grid), O.interior(ou, grid), O.interior(ov, grid)
+    d_o = np.abs(oui.astype(np.float64) - ovi)
+    du = np.abs(ui.astype(np.float64) - oui)
+    ulp = ULP[storage]
+    # per plane: a floor below the plane's own values (each side of the jump)
+    floor = 2.0 ** -30 * np.max(np.abs(oui), axis=(1, 2), keepdims=True)
+    assert np.all(du <= ulp * (np.abs(oui) + d_o) + floor)
