@@ -580,9 +580,9 @@ int plan_tma16(st3d_ctx* c, int sm_count, int max_smem) {
 // The tensor-core kernel serves a delta-form request when asked for, or under
 // ST3D_KERNEL_AUTO when the request names no tile height or pipeline depth of
 // the scalar kernel: measured at 1024^3 on a GB300 it is the faster kernel
-// of the delta forms (25 points FP16 457 against 317 Gpts/s, BF16 446 / 312,
-// F16_HL 395 / 283; 13 points (1040^3) FP16 512 / 408, F16_HL 407 / 363;
-// 7 points FP16 612 / 545, BF16 592 / 531, F16_HL 416 / 357).
+// of the delta forms (25 points FP16 515 against 317 Gpts/s, BF16 498 / 312,
+// F16_HL 397 / 283; 13 points (1040^3) FP16 500 / 408, F16_HL 410 / 363;
+// 7 points FP16 615 / 545, BF16 603 / 531, F16_HL 418 / 357).
 bool mma_chosen(const st3d_opts& o) {
   const bool delta = o.storage == ST3D_F16 || o.storage == ST3D_BF16 || o.storage == ST3D_F16_HL;
   if (!delta || o.mode != ST3D_MODE_WAVE) return false;
