@@ -28,10 +28,10 @@
 // The per-plane weights, 2^X-scaled factors c1 w_r 2^X, 2^Y and the step's
 // other scales form one 128-byte record per plane, written before each step
 // by k_mma_records and brought into the stage by the producer with one bulk
-// copy.  The u
-// planes i-R .. i+R all stay in the shared-memory ring (16 slots >= 8 stages
-// + 2R), so no register queue along i is needed.  The centre u (and, for the
-// pair form, its lo words) is decoded in FP32 for u^{n+1} = u + dec(enc(d)).
+// copy.  The u planes i-R .. i+R all stay in the shared-memory ring (16 slots
+// >= 8 stages + 2R), so no register queue along i is needed.  The centre u
+// (and, for the pair form, its lo words) is decoded in FP32 for
+// u^{n+1} = u + dec(enc(d)).
 //
 // The tensor cores sum the products in their own order and rounding, so this
 // kernel is not bit-identical to the scalar one or to the oracle's
@@ -50,18 +50,18 @@
 // consumer warps each own one 16x8 block (20 warps with the producer: five
 // on some schedulers, within the 96 registers a thread that leaves; the
 // kernel takes 81-87).  The row pitches (336 and 304 bytes) put the eight
-// rows of every ldmatrix in distinct banks.  Each warp writes its block of u^{n+1},
-// d^{n+1} (and the lo words) into the stage's s, d (and lo) slots, whose
+// rows of every ldmatrix in distinct banks.  Each warp writes its block of
+// u^{n+1}, d^{n+1} (and the lo words) into the stage's s, d (and lo) slots, whose
 // inputs it has read, with zero words at the points outside the grid; once
 // every warp has released the stage the producer stores the three tiles with
 // TMA (whole lines, clipped by the tensor maps' extents) and waits for the
 // stores to read shared memory before it loads the slots again.  A store
 // whose clipped row ends inside a 16-byte segment was seen to write the rest
 // of that segment (the zero halo along k when zs is not a multiple of 8), so
-// the outputs outside the grid are zeros, the value the halo holds.  Waits are bounded; after a timeout the
-// consumers keep stepping and arriving without waiting, so that the
-// producer's bounded drain ends and every CTA returns (the status word marks
-// the results void).
+// the outputs outside the grid are zeros, the value the halo holds.  Waits
+// are bounded; after a timeout the consumers keep stepping and arriving
+// without waiting, so that the producer's bounded drain ends and every CTA
+// returns (the status word marks the results void).
 #include <math.h>
 #include <string.h>
 
