@@ -178,6 +178,31 @@ def test_plan_reports_the_tensor_core_kernel():
     assert auto(25, "f16_hilo") == auto(25, "f32") == S.KERNEL_TMA
 
 
+@pytest.mark.parametrize("storage,eb", [("f32", 4), ("f64", 8), ("f16", 2), ("bf16", 2),
+                                        ("f16_hl", 2), ("f16_hilo", 2)])
+@pytest.mark.parametrize("points", [7, 25])
+@pytest.mark.parametrize("shape", [(17, 19, 23), (9, 17, 141), (30, 43, 140), (64, 40, 1000)])
+def test_layout_keeps_tile_origins_16_byte_aligned(storage, eb, points, shape):
+    """A TMA tile copy faults unless its innermost coordinate times the word
+    size is a multiple of 16 bytes.  The layout starts the interior one
+    128-byte pad into each row and makes rows whole 128-byte lines; the tile
+    kernels take columns k0 - kh .. with k0 a multiple of the tile width and
+    kh their k margin (4 or 8 floats for FP32, 8 words for 16-bit tiles).
+    Every such origin over the grid's tiles, and every store origin k0,
+    falls on a 16-byte boundary."""
+    info = S.plan(S.Grid(*shape, 4, 4, 4), S.default_opts(points, "wave", storage))
+    assert info.pk * eb == 128 and (info.nk * eb) % 128 == 0
+    assert info.nk >= info.pk + shape[2] + 8
+    if info.tile_k == 0:
+        assert info.kernel == S.KERNEL_SIMPLE
+        return
+    assert (info.tile_k * eb) % 16 == 0
+    for kh in ((4, 8) if eb == 4 else (8,)):
+        for k0 in range(0, shape[2], info.tile_k):
+            assert ((info.pk + k0 - kh) * eb) % 16 == 0
+            assert ((info.pk + k0) * eb) % 16 == 0
+
+
 def test_device_field_defaults_and_planning():
     """opts.device: -1 (the current device) by default; st3d_plan reports
     the requested ordinal and rejects one below -1."""
